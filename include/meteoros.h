@@ -1,0 +1,246 @@
+/*
+ * meteoros.h — C ABI of the GB300-native Meteoros compute stage.
+ *
+ * This library replaces the reference renderer's per-frame compute command
+ * buffer (Renderer.cpp:653-722): the reprojection dispatch
+ * (shaders/reprojection.comp) and the cloud raymarch dispatch
+ * (shaders/cloudRayMarch.comp), plus the TXAA resolve
+ * (shaders/postProcess_TXAA.frag) and the noise volumes that the reference
+ * loads from disk (Sky.cpp:25-58).  All entry points are plain C: pointers,
+ * sizes and status codes.  No C++ exception crosses this boundary.
+ *
+ * Threading: one mt_ctx per host thread.  Calls on one context are ordered on
+ * the CUDA stream passed in (NULL = the legacy default stream).  Distinct
+ * contexts may be used concurrently from different threads.
+ *
+ * Image layout: every image is row-major, row 0 first, with no padding.  An
+ * RGBA image is width*height*4 floats (RGBA32F); a mask is width*height floats
+ * (R32F).  Pixel (x, y) is GLSL imageLoad/imageStore coordinate ivec2(x, y).
+ */
+#ifndef METEOROS_H
+#define METEOROS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define MT_API __attribute__((visibility("default")))
+#else
+#define MT_API
+#endif
+
+#define MT_ABI_VERSION 1
+
+/* Noise volume sizes.  Fixed by the reference's asset set:
+ * Sky.cpp:31 (128^3 RGBA8 base shape), Sky.cpp:40 (32^3 RGBA8 detail),
+ * Sky.cpp:47 (128^2 RGBA8 curl), Sky.cpp:54 (512^2 RGBA8 weather map). */
+#define MT_BASE_N 128
+#define MT_DETAIL_N 32
+#define MT_CURL_N 128
+#define MT_WEATHER_N 512
+#define MT_MAX_WEATHER_SLOTS 256
+#define MT_MAX_DIM 16384
+
+/* Status codes.  The reference throws std::runtime_error on a VkResult other
+ * than VK_SUCCESS (Renderer.cpp:139-141, 430-432); here each call returns one
+ * of these, and mt_last_error() gives the message. */
+typedef enum mt_status {
+    MT_OK = 0,
+    MT_ERR_INVALID_ARG = 1,  /* null pointer, bad size, bad slot, bad flags */
+    MT_ERR_NO_VOLUMES = 2,   /* render before any volume upload/generation */
+    MT_ERR_CUDA = 3,         /* a CUDA runtime call failed */
+    MT_ERR_OUT_OF_MEMORY = 4,
+    MT_ERR_UNSUPPORTED = 5,  /* e.g. no sm_103a device */
+    MT_ERR_BUDGET = 6,       /* serving: request does not fit the HBM budget */
+    MT_ERR_TIMEOUT = 7       /* a bounded wait gave up */
+} mt_status;
+
+/* CameraUBO: camera.h:12-18 and cloudRayMarch.comp:15-21 (std140, 152 bytes,
+ * padded here to 160).  Matrices are column-major: view[c*4 + r] is GLSL
+ * view[c][r], as glm stores them. */
+typedef struct mt_camera_ubo {
+    float view[16];
+    float proj[16];
+    float eye[4];
+    float tan_fov_by_2[2]; /* .x = aspect * tan(fovy/2), .y = tan(fovy/2) */
+    float _pad[2];
+} mt_camera_ubo;
+
+/* TimeUBO: Scene.h:12-21 and cloudRayMarch.comp:23-31 (std140, 80 bytes). */
+typedef struct mt_time_ubo {
+    float halton_seq1[4];
+    float halton_seq2[4];
+    float halton_seq3[4];
+    float halton_seq4[4];
+    float time[2]; /* .x = delta time, .y = total time (seconds) */
+    int32_t frame_count_mod16;
+    int32_t _pad;
+} mt_time_ubo;
+
+/* Storage precision of the noise volumes read by the raymarch. */
+typedef enum mt_storage {
+    MT_STORAGE_U8 = 0,   /* RGBA8 UNORM, as the reference's textures */
+    MT_STORAGE_F16 = 1,  /* precision form: IEEE half volumes, half2 density math */
+    MT_STORAGE_BF16 = 2  /* precision form: bfloat16 volumes, half2 density math */
+} mt_storage;
+
+/* Render flags. */
+#define MT_RENDER_CHECKERBOARD 0u /* 1 pixel per 4x4 block marched, the rest reprojected (the reference) */
+#define MT_RENDER_FULL 1u         /* every pixel marched, no reprojection (config 0) */
+#define MT_RENDER_COUNT 2u        /* accumulate executed-sample counters (mt_get_stats) */
+
+/* Parameters the reference compiles in as #defines and literals.
+ * mt_params_reference() fills the reference's values; mt_params_config()
+ * fills the physically parameterised values of the benchmark configurations.
+ * Both run the same kernels. */
+typedef struct mt_params {
+    /* Atmosphere shells: cloudRayMarch.comp:75-78 */
+    float earth_radius;        /* EARTH_RADIUS */
+    float shell_inner_radius;  /* ATMOSPHERE_RADIUS_INNER (from the Earth's centre) */
+    float shell_outer_radius;  /* ATMOSPHERE_RADIUS_OUTER */
+    float noise_period;        /* samplePoint /= 8.0 (cloudRayMarch.comp:635) */
+    /* Primary march: cloudRayMarch.comp:572, 680-684 */
+    int32_t steps_min;         /* floor(mix(steps_min, steps_max, 1 - dir.y)); equal = fixed */
+    int32_t steps_max;
+    float accum_limit;         /* stop once accumulated density >= accum_limit (1.0 in the reference) */
+    /* Coverage / weather map: cloudRayMarch.comp:515-537 */
+    int32_t coverage_mode;     /* 0: constant `coverage`; 1: weather map R with threshold 1 - R */
+    float coverage;            /* cloud_coverage = 0.6 */
+    int32_t height_gradient;   /* 1: multiply by getDensityHeightGradientForPoint(h, weather B) */
+    float weather_scale;       /* weather uv = (pos - earthCentre).xz / weather_scale */
+    int32_t weather_slot;      /* which uploaded/generated weather map to read */
+    /* Wind: cloudRayMarch.comp:88-91, 489-497 */
+    float wind_dir[3];         /* WIND_DIRECTION + vec3(0, 0.1, 0) */
+    float wind_speed;          /* CLOUD_SPEED (noise units per second) */
+    float skew_dir[3];         /* WIND_DIRECTION for the top skew */
+    float cloud_top_offset;    /* CLOUD_TOP_OFFSET (times 0.009) */
+    /* Sun: cloudRayMarch.comp:93-99 */
+    float sun_light_pos[3];    /* SUN_LOCATION: lights the clouds */
+    float sky_sun_pos[3];      /* BACKGROUND_SKY_SUN_LOCATION: Preetham sky */
+    float eye_sign;            /* ray origin = eye_sign * camera.eye (-1 in the reference, :707) */
+    /* TXAA feedback: postProcess_TXAA.frag:52-53 */
+    float feedback_min;
+    float feedback_max;
+    /* Checkerboard slot order: cloudRayMarch.comp:695-701 (slot i -> (i/4, i%4)) */
+    int32_t slot_x[16];
+    int32_t slot_y[16];
+    /* Precision form */
+    int32_t storage;           /* mt_storage */
+    int32_t fp64_shells;       /* 1: shell intersection in FP64 (precision form) */
+    int32_t _reserved[7];
+} mt_params;
+
+/* Counters of the last render call made with MT_RENDER_COUNT. */
+typedef struct mt_stats {
+    uint64_t primary_samples; /* executed iterations of cloudRayMarch.comp:627-686 */
+    uint64_t light_samples;   /* executed cone-light base-shape fetches (:654-668) */
+    uint64_t marched_rays;    /* rays that reached the march loop */
+    uint64_t pixels;          /* pixels written (marched + reprojected + horizon) */
+} mt_stats;
+
+/* One view of a batched render (config 3). */
+typedef struct mt_view {
+    mt_camera_ubo camera;
+    mt_camera_ubo camera_old;
+    mt_time_ubo time;
+    mt_params params;
+    const float* prev_rgba;  /* device, may be NULL with MT_RENDER_FULL */
+    float* cur_rgba;         /* device */
+    float* godray_mask;      /* device, may be NULL */
+    int32_t width;
+    int32_t height;
+    uint32_t flags;
+    int32_t _pad;
+} mt_view;
+
+typedef struct mt_ctx mt_ctx;
+
+/* ---- library / context -------------------------------------------------- */
+
+MT_API int mt_abi_version(void);
+
+/* Replaces VulkanInstance/VulkanDevice creation (main.cpp:135-156) for the
+ * compute path: binds CUDA device `device` and checks it is sm_103. */
+MT_API mt_status mt_create(mt_ctx** out, int device);
+MT_API void mt_destroy(mt_ctx* ctx);
+/* Message of the last failed call on ctx (or of the last failed mt_create when
+ * ctx is NULL).  Never NULL. */
+MT_API const char* mt_last_error(const mt_ctx* ctx);
+
+/* ---- parameters and uniform producers (host only, no GPU work) ---------- */
+
+MT_API void mt_params_reference(mt_params* out);
+MT_API void mt_params_config(mt_params* out);
+/* Scene::InitializeTime (Scene.cpp:86-119): Halton base 3, i = 1..16;
+ * frame count 0; time zero. */
+MT_API void mt_time_init(mt_time_ubo* out);
+/* Scene::UpdateTime (Scene.cpp:65-85): time.x = dt, time.y += dt,
+ * frameCount = (frameCount + 1) % 16. */
+MT_API void mt_time_advance(mt_time_ubo* t, float dt);
+/* Camera::UpdateBuffer (camera.cpp:31-42): view = lookAt(eye, ref, up),
+ * proj = perspective with proj[1][1] negated, eye, tan(fovy/2). */
+MT_API void mt_camera_look_at(mt_camera_ubo* out, const float eye[3], const float ref[3],
+                              float fovy_deg, float aspect, float near_clip, float far_clip);
+/* Scene::HaltonSequenceAt (Scene.cpp:125-138). */
+MT_API float mt_halton(int index, int base);
+
+/* ---- noise volumes (Sky::CreateCloudResources, Sky.cpp:25-58) ----------- */
+
+/* Upload RGBA8 volumes from host memory, in create3DTextureFromMany2DTextures
+ * layout (ImageLoadingUtility.cpp:75-139: x fastest, then y, then slice z).
+ * Any pointer may be NULL to keep the current volume.  `weather` goes to slot 0. */
+MT_API mt_status mt_upload_volumes(mt_ctx* ctx, const uint8_t* base_rgba8, const uint8_t* detail_rgba8,
+                                   const uint8_t* curl_rgba8, const uint8_t* weather_rgba8);
+MT_API mt_status mt_upload_weather(mt_ctx* ctx, int slot, const uint8_t* weather_rgba8);
+/* Generate the four noise volumes on the GPU from `seed` (no reference
+ * counterpart: the reference loads pre-baked assets).  Writes RGBA8 and the
+ * FP16/BF16 precision-form copies.  Weather goes to slot 0. */
+MT_API mt_status mt_generate_volumes(mt_ctx* ctx, uint64_t seed, void* stream);
+MT_API mt_status mt_generate_weather(mt_ctx* ctx, int slot, uint64_t seed, void* stream);
+/* Copy volumes back to host memory (any pointer may be NULL). */
+MT_API mt_status mt_download_volumes(mt_ctx* ctx, uint8_t* base_rgba8, uint8_t* detail_rgba8,
+                                     uint8_t* curl_rgba8, uint8_t* weather_rgba8, int weather_slot);
+/* Copy the half-precision copies back (raw IEEE half or bfloat16 bits). */
+MT_API mt_status mt_download_volumes_16(mt_ctx* ctx, int storage, uint16_t* base_rgba, uint16_t* detail_rgba,
+                                        uint16_t* curl_rgba, uint16_t* weather_rgba, int weather_slot);
+
+/* ---- the compute stage -------------------------------------------------- */
+
+/* One compute command buffer of the reference (Renderer.cpp:653-722): with
+ * MT_RENDER_CHECKERBOARD, every pixel of cur_rgba is the 10-tap reprojection of
+ * prev_rgba (reprojection.comp:193-244) except the one pixel per 4x4 block
+ * selected by time->frame_count_mod16, which is raymarched
+ * (cloudRayMarch.comp:690-826).  With MT_RENDER_FULL every pixel is marched
+ * and prev_rgba is not read.  godray_mask (may be NULL) receives, for each
+ * marched pixel only, the scalar the god-ray pass decodes
+ * (postProcess_GodRays.frag:39-43); other mask pixels keep their contents, as
+ * the reference's god-ray image does.  Device pointers; stream-ordered. */
+MT_API mt_status mt_render(mt_ctx* ctx, const mt_camera_ubo* camera, const mt_camera_ubo* camera_old,
+                           const mt_time_ubo* time, const mt_params* params, const float* prev_rgba,
+                           float* cur_rgba, float* godray_mask, int width, int height, uint32_t flags,
+                           void* stream);
+
+/* TXAA resolve (postProcess_TXAA.frag:223-269) of `current` against
+ * `history` (the previous resolved frame), written to `out` (distinct from
+ * both).  Device pointers; stream-ordered. */
+MT_API mt_status mt_txaa(mt_ctx* ctx, const mt_camera_ubo* camera, const mt_camera_ubo* camera_old,
+                         const mt_time_ubo* time, const mt_params* params, const float* current_rgba,
+                         const float* history_rgba, float* out_rgba, int width, int height, void* stream);
+
+/* Many views, uneven sizes, one persistent launch (config 3).  `views` is a
+ * host array; its image pointers are device pointers. */
+MT_API mt_status mt_render_batch(mt_ctx* ctx, const mt_view* views, int n_views, void* stream);
+
+/* Counters accumulated by render calls made with MT_RENDER_COUNT since the
+ * last reset.  Synchronises the stream. */
+MT_API mt_status mt_get_stats(mt_ctx* ctx, mt_stats* out, int reset, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* METEOROS_H */
