@@ -142,6 +142,16 @@ typedef struct mt_stats {
     uint64_t pixels;          /* pixels written (marched + reprojected + horizon) */
 } mt_stats;
 
+/* Device durations of the most recent launches made while timing was on
+ * (mt_set_timing).  A kernel that did not run since timing was switched on
+ * reads 0. */
+typedef struct mt_kernel_times {
+    float reproject_ms;
+    float march_ms;
+    float txaa_ms;
+    int32_t _pad;
+} mt_kernel_times;
+
 /* One view of a batched render (config 3). */
 typedef struct mt_view {
     mt_camera_ubo camera;
@@ -238,6 +248,13 @@ MT_API mt_status mt_render_batch(mt_ctx* ctx, const mt_view* views, int n_views,
 /* Counters accumulated by render calls made with MT_RENDER_COUNT since the
  * last reset.  Synchronises the stream. */
 MT_API mt_status mt_get_stats(mt_ctx* ctx, mt_stats* out, int reset, void* stream);
+
+/* Per-kernel CUDA-event timing (no counterpart in the reference, which only
+ * reports frame rates read off externally, README.md:266-294).  While on,
+ * each kernel launch is bracketed by events on its stream. */
+MT_API mt_status mt_set_timing(mt_ctx* ctx, int enabled);
+/* Synchronises on the recorded events and returns their durations. */
+MT_API mt_status mt_get_kernel_times(mt_ctx* ctx, mt_kernel_times* out);
 
 #ifdef __cplusplus
 }

@@ -105,6 +105,11 @@ class Stats(C.Structure):
     ]
 
 
+class KernelTimes(C.Structure):
+    _fields_ = [("reproject_ms", C.c_float), ("march_ms", C.c_float), ("txaa_ms", C.c_float),
+                ("_pad", C.c_int32)]
+
+
 class View(C.Structure):
     _fields_ = [
         ("camera", CameraUBO),
@@ -151,6 +156,8 @@ SIGNATURES = {
                           C.POINTER(Params), _P, _P, _P, C.c_int, C.c_int, _P]),
     "mt_render_batch": (C.c_int, [_P, C.POINTER(View), C.c_int, _P]),
     "mt_get_stats": (C.c_int, [_P, C.POINTER(Stats), C.c_int, _P]),
+    "mt_set_timing": (C.c_int, [_P, C.c_int]),
+    "mt_get_kernel_times": (C.c_int, [_P, C.POINTER(KernelTimes)]),
 }
 
 _lib = None

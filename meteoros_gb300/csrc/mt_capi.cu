@@ -1,0 +1,451 @@
+// The C ABI of include/meteoros.h: context, volume ownership, argument
+// checking and kernel dispatch.
+//
+// Replaces, on the compute path:
+//   Renderer::RecordComputeCommandBuffer / Frame  (Renderer.cpp:653-722, 122-141)
+//   Sky::CreateCloudResources                    (Sky.cpp:25-58)
+//   the descriptor sets binding images, samplers and uniform blocks
+//                                                (Renderer.cpp:914-1086)
+// Errors: every entry point returns an mt_status and records a message that
+// mt_last_error() returns; no exception crosses the boundary.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "mt_kernels.h"
+
+struct mt_ctx {
+    int device = 0;
+    std::string err;
+    uint32_t* base = nullptr;
+    uint32_t* detail = nullptr;
+    uint32_t* curl = nullptr;
+    uint2* base16[2] = {nullptr, nullptr};    // [0] IEEE half, [1] bfloat16
+    uint2* detail16[2] = {nullptr, nullptr};
+    uint2* curl16[2] = {nullptr, nullptr};
+    std::vector<uint32_t*> weather;           // MT_MAX_WEATHER_SLOTS entries, allocated on demand
+    std::vector<uint2*> weather16[2];
+    bool have_base = false, have_detail = false, have_curl = false;
+    unsigned long long* stats = nullptr;      // 4 counters
+    bool timing = false;
+    cudaEvent_t ev[6] = {};                   // reproject, march, txaa (start, end)
+    bool ran[3] = {false, false, false};
+};
+
+namespace {
+
+thread_local std::string g_create_error;
+
+constexpr size_t kBaseTexels = (size_t)MT_BASE_N * MT_BASE_N * MT_BASE_N;
+constexpr size_t kDetailTexels = (size_t)MT_DETAIL_N * MT_DETAIL_N * MT_DETAIL_N;
+constexpr size_t kCurlTexels = (size_t)MT_CURL_N * MT_CURL_N;
+constexpr size_t kWeatherTexels = (size_t)MT_WEATHER_N * MT_WEATHER_N;
+
+mt_status fail(mt_ctx* ctx, mt_status st, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (ctx)
+        ctx->err = buf;
+    else
+        g_create_error = buf;
+    return st;
+}
+
+#define MT_CUDA(ctx, call)                                                                                 \
+    do {                                                                                                   \
+        cudaError_t e_ = (call);                                                                           \
+        if (e_ != cudaSuccess)                                                                             \
+            return fail((ctx), e_ == cudaErrorMemoryAllocation ? MT_ERR_OUT_OF_MEMORY : MT_ERR_CUDA,       \
+                        "%s failed: %s", #call, cudaGetErrorString(e_));                                   \
+    } while (0)
+
+template <class T> mt_status alloc(mt_ctx* ctx, T** p, size_t count) {
+    if (*p) return MT_OK;
+    MT_CUDA(ctx, cudaMalloc((void**)p, count * sizeof(T)));
+    return MT_OK;
+}
+
+mt_status bind_device(mt_ctx* ctx) {
+    MT_CUDA(ctx, cudaSetDevice(ctx->device));
+    return MT_OK;
+}
+
+bool aligned(const void* p, size_t a) { return ((uintptr_t)p % a) == 0; }
+
+mt_status check_params(mt_ctx* ctx, const mt_params* p, const mt_time_ubo* t) {
+    if (!p || !t) return fail(ctx, MT_ERR_INVALID_ARG, "params and time must not be NULL");
+    if (t->frame_count_mod16 < 0 || t->frame_count_mod16 > 15)
+        return fail(ctx, MT_ERR_INVALID_ARG, "time.frame_count_mod16 = %d is outside 0..15", t->frame_count_mod16);
+    if (!(p->earth_radius > 0.0f) || !(p->shell_inner_radius > p->earth_radius) ||
+        !(p->shell_outer_radius > p->shell_inner_radius))
+        return fail(ctx, MT_ERR_INVALID_ARG, "shell radii must satisfy 0 < earth < inner < outer");
+    if (!(p->noise_period > 0.0f)) return fail(ctx, MT_ERR_INVALID_ARG, "noise_period must be > 0");
+    if (p->steps_min < 1 || p->steps_max < 1 || p->steps_min > 4096 || p->steps_max > 4096)
+        return fail(ctx, MT_ERR_INVALID_ARG, "steps_min/steps_max must be in 1..4096");
+    if (p->coverage_mode != 0 && p->coverage_mode != 1)
+        return fail(ctx, MT_ERR_INVALID_ARG, "coverage_mode must be 0 or 1");
+    if (p->coverage_mode == 1 && !(p->weather_scale > 0.0f))
+        return fail(ctx, MT_ERR_INVALID_ARG, "weather_scale must be > 0");
+    if (p->weather_slot < 0 || p->weather_slot >= MT_MAX_WEATHER_SLOTS)
+        return fail(ctx, MT_ERR_INVALID_ARG, "weather_slot %d is outside 0..%d", p->weather_slot,
+                    MT_MAX_WEATHER_SLOTS - 1);
+    for (int i = 0; i < 16; ++i)
+        if (p->slot_x[i] < 0 || p->slot_x[i] > 3 || p->slot_y[i] < 0 || p->slot_y[i] > 3)
+            return fail(ctx, MT_ERR_INVALID_ARG, "checkerboard slot %d is outside the 4x4 block", i);
+    if (p->storage != MT_STORAGE_U8 && p->storage != MT_STORAGE_F16 && p->storage != MT_STORAGE_BF16)
+        return fail(ctx, MT_ERR_INVALID_ARG, "unknown storage %d", p->storage);
+    return MT_OK;
+}
+
+mt_status check_image(mt_ctx* ctx, int w, int h) {
+    if (w < 1 || h < 1 || w > MT_MAX_DIM || h > MT_MAX_DIM)
+        return fail(ctx, MT_ERR_INVALID_ARG, "image size %dx%d is outside 1..%d", w, h, MT_MAX_DIM);
+    return MT_OK;
+}
+
+mt_status ensure_weather(mt_ctx* ctx, int slot) {
+    if (ctx->weather[slot]) return MT_OK;
+    mt_status st = alloc(ctx, &ctx->weather[slot], kWeatherTexels);
+    if (st != MT_OK) return st;
+    st = alloc(ctx, &ctx->weather16[0][slot], kWeatherTexels);
+    if (st != MT_OK) return st;
+    return alloc(ctx, &ctx->weather16[1][slot], kWeatherTexels);
+}
+
+mt_status ensure_volumes(mt_ctx* ctx) {
+    mt_status st;
+    if ((st = alloc(ctx, &ctx->base, kBaseTexels)) != MT_OK) return st;
+    if ((st = alloc(ctx, &ctx->detail, kDetailTexels)) != MT_OK) return st;
+    if ((st = alloc(ctx, &ctx->curl, kCurlTexels)) != MT_OK) return st;
+    for (int k = 0; k < 2; ++k) {
+        if ((st = alloc(ctx, &ctx->base16[k], kBaseTexels)) != MT_OK) return st;
+        if ((st = alloc(ctx, &ctx->detail16[k], kDetailTexels)) != MT_OK) return st;
+        if ((st = alloc(ctx, &ctx->curl16[k], kCurlTexels)) != MT_OK) return st;
+    }
+    return MT_OK;
+}
+
+uint32_t seed32(uint64_t s) { return (uint32_t)s ^ (uint32_t)(s >> 32); }
+
+mt_status build_march_args(mt_ctx* ctx, const mt_camera_ubo* cam, const mt_camera_ubo* cam_old,
+                           const mt_time_ubo* tm, const mt_params* p, const float* prev, float* cur, float* mask,
+                           int w, int h, uint32_t flags, mt::MarchArgs* a) {
+    if (!cam || !cam_old) return fail(ctx, MT_ERR_INVALID_ARG, "camera and camera_old must not be NULL");
+    mt_status st;
+    if ((st = check_params(ctx, p, tm)) != MT_OK) return st;
+    if ((st = check_image(ctx, w, h)) != MT_OK) return st;
+    if (flags & ~(MT_RENDER_FULL | MT_RENDER_COUNT)) return fail(ctx, MT_ERR_INVALID_ARG, "unknown flags 0x%x", flags);
+    if (!cur) return fail(ctx, MT_ERR_INVALID_ARG, "cur_rgba must not be NULL");
+    if (!aligned(cur, 16) || (prev && !aligned(prev, 16)) || (mask && !aligned(mask, 4)))
+        return fail(ctx, MT_ERR_INVALID_ARG, "images must be 16-byte aligned (mask 4-byte)");
+    const bool full = (flags & MT_RENDER_FULL) != 0;
+    if (!full && !prev) return fail(ctx, MT_ERR_INVALID_ARG, "prev_rgba is required without MT_RENDER_FULL");
+    if (!full && prev == cur) return fail(ctx, MT_ERR_INVALID_ARG, "prev_rgba and cur_rgba must be distinct images");
+    if (!ctx->have_base || !ctx->have_detail || !ctx->have_curl)
+        return fail(ctx, MT_ERR_NO_VOLUMES, "noise volumes have not been uploaded or generated");
+    if (p->coverage_mode == 1 && !ctx->weather[p->weather_slot])
+        return fail(ctx, MT_ERR_NO_VOLUMES, "weather slot %d holds no weather map", p->weather_slot);
+    if (p->storage != MT_STORAGE_U8)
+        return fail(ctx, MT_ERR_UNSUPPORTED, "storage %d is not available in this build", p->storage);
+    std::memset(a, 0, sizeof(*a));
+    a->camera = *cam;
+    a->camera_old = *cam_old;
+    a->time = *tm;
+    a->params = *p;
+    a->base = ctx->base;
+    a->detail = ctx->detail;
+    a->curl = ctx->curl;
+    a->weather = ctx->weather[p->weather_slot] ? ctx->weather[p->weather_slot] : ctx->curl;
+    if (p->coverage_mode == 0) a->weather = ctx->curl;  // never read
+    a->prev = (const float4*)prev;
+    a->cur = (float4*)cur;
+    a->mask = mask;
+    a->stats = (flags & MT_RENDER_COUNT) ? ctx->stats : nullptr;
+    a->width = w;
+    a->height = h;
+    a->groups_x = mt::march_groups(w);
+    a->groups_y = mt::march_groups(h);
+    a->flags = flags;
+    return MT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+MT_API mt_status mt_create(mt_ctx** out, int device) {
+    if (!out) return fail(nullptr, MT_ERR_INVALID_ARG, "out must not be NULL");
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0)
+        return fail(nullptr, MT_ERR_UNSUPPORTED, "no CUDA device: %s", cudaGetErrorString(e));
+    if (device < 0 || device >= n) return fail(nullptr, MT_ERR_INVALID_ARG, "device %d of %d", device, n);
+    cudaDeviceProp prop;
+    e = cudaGetDeviceProperties(&prop, device);
+    if (e != cudaSuccess) return fail(nullptr, MT_ERR_CUDA, "cudaGetDeviceProperties: %s", cudaGetErrorString(e));
+    if (prop.major != 10 || prop.minor != 3)
+        return fail(nullptr, MT_ERR_UNSUPPORTED, "device %d is sm_%d%d; this library is built for sm_103a", device,
+                    prop.major, prop.minor);
+    mt_ctx* ctx = new (std::nothrow) mt_ctx();
+    if (!ctx) return fail(nullptr, MT_ERR_OUT_OF_MEMORY, "host allocation failed");
+    ctx->device = device;
+    ctx->weather.assign(MT_MAX_WEATHER_SLOTS, nullptr);
+    ctx->weather16[0].assign(MT_MAX_WEATHER_SLOTS, nullptr);
+    ctx->weather16[1].assign(MT_MAX_WEATHER_SLOTS, nullptr);
+    if (bind_device(ctx) != MT_OK || alloc(ctx, &ctx->stats, 4) != MT_OK ||
+        cudaMemset(ctx->stats, 0, 4 * sizeof(unsigned long long)) != cudaSuccess) {
+        g_create_error = ctx->err.empty() ? "context set-up failed" : ctx->err;
+        mt_destroy(ctx);
+        return MT_ERR_CUDA;
+    }
+    *out = ctx;
+    return MT_OK;
+}
+
+MT_API void mt_destroy(mt_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    cudaFree(ctx->base);
+    cudaFree(ctx->detail);
+    cudaFree(ctx->curl);
+    for (int k = 0; k < 2; ++k) {
+        cudaFree(ctx->base16[k]);
+        cudaFree(ctx->detail16[k]);
+        cudaFree(ctx->curl16[k]);
+        for (uint2* w : ctx->weather16[k]) cudaFree(w);
+    }
+    for (uint32_t* w : ctx->weather) cudaFree(w);
+    cudaFree(ctx->stats);
+    for (cudaEvent_t e : ctx->ev)
+        if (e) cudaEventDestroy(e);
+    delete ctx;
+}
+
+MT_API const char* mt_last_error(const mt_ctx* ctx) {
+    if (!ctx) return g_create_error.c_str();
+    return ctx->err.c_str();
+}
+
+MT_API mt_status mt_upload_volumes(mt_ctx* ctx, const uint8_t* base, const uint8_t* detail, const uint8_t* curl,
+                                   const uint8_t* weather) {
+    if (!ctx) return MT_ERR_INVALID_ARG;
+    mt_status st;
+    if ((st = bind_device(ctx)) != MT_OK) return st;
+    if ((st = ensure_volumes(ctx)) != MT_OK) return st;
+    if (base) {
+        MT_CUDA(ctx, cudaMemcpy(ctx->base, base, kBaseTexels * 4, cudaMemcpyHostToDevice));
+        MT_CUDA(ctx, mt::launch_u8_to_16(ctx->base, kBaseTexels, ctx->base16[0], ctx->base16[1], 0));
+        ctx->have_base = true;
+    }
+    if (detail) {
+        MT_CUDA(ctx, cudaMemcpy(ctx->detail, detail, kDetailTexels * 4, cudaMemcpyHostToDevice));
+        MT_CUDA(ctx, mt::launch_u8_to_16(ctx->detail, kDetailTexels, ctx->detail16[0], ctx->detail16[1], 0));
+        ctx->have_detail = true;
+    }
+    if (curl) {
+        MT_CUDA(ctx, cudaMemcpy(ctx->curl, curl, kCurlTexels * 4, cudaMemcpyHostToDevice));
+        MT_CUDA(ctx, mt::launch_u8_to_16(ctx->curl, kCurlTexels, ctx->curl16[0], ctx->curl16[1], 0));
+        ctx->have_curl = true;
+    }
+    if (weather) {
+        if ((st = mt_upload_weather(ctx, 0, weather)) != MT_OK) return st;
+    }
+    MT_CUDA(ctx, cudaDeviceSynchronize());
+    return MT_OK;
+}
+
+MT_API mt_status mt_upload_weather(mt_ctx* ctx, int slot, const uint8_t* weather) {
+    if (!ctx) return MT_ERR_INVALID_ARG;
+    if (!weather) return fail(ctx, MT_ERR_INVALID_ARG, "weather must not be NULL");
+    if (slot < 0 || slot >= MT_MAX_WEATHER_SLOTS) return fail(ctx, MT_ERR_INVALID_ARG, "weather slot %d", slot);
+    mt_status st;
+    if ((st = bind_device(ctx)) != MT_OK) return st;
+    if ((st = ensure_weather(ctx, slot)) != MT_OK) return st;
+    MT_CUDA(ctx, cudaMemcpy(ctx->weather[slot], weather, kWeatherTexels * 4, cudaMemcpyHostToDevice));
+    MT_CUDA(ctx, mt::launch_u8_to_16(ctx->weather[slot], kWeatherTexels, ctx->weather16[0][slot],
+                                     ctx->weather16[1][slot], 0));
+    MT_CUDA(ctx, cudaDeviceSynchronize());
+    return MT_OK;
+}
+
+MT_API mt_status mt_generate_volumes(mt_ctx* ctx, uint64_t seed, void* stream) {
+    if (!ctx) return MT_ERR_INVALID_ARG;
+    mt_status st;
+    if ((st = bind_device(ctx)) != MT_OK) return st;
+    if ((st = ensure_volumes(ctx)) != MT_OK) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint32_t s32 = seed32(seed);
+    MT_CUDA(ctx, mt::launch_generate_base(s32, mt::NoiseOut{ctx->base, ctx->base16[0], ctx->base16[1]}, s));
+    MT_CUDA(ctx, mt::launch_generate_detail(s32, mt::NoiseOut{ctx->detail, ctx->detail16[0], ctx->detail16[1]}, s));
+    MT_CUDA(ctx, mt::launch_generate_curl(s32, mt::NoiseOut{ctx->curl, ctx->curl16[0], ctx->curl16[1]}, s));
+    ctx->have_base = ctx->have_detail = ctx->have_curl = true;
+    return mt_generate_weather(ctx, 0, seed, stream);
+}
+
+MT_API mt_status mt_generate_weather(mt_ctx* ctx, int slot, uint64_t seed, void* stream) {
+    if (!ctx) return MT_ERR_INVALID_ARG;
+    if (slot < 0 || slot >= MT_MAX_WEATHER_SLOTS) return fail(ctx, MT_ERR_INVALID_ARG, "weather slot %d", slot);
+    mt_status st;
+    if ((st = bind_device(ctx)) != MT_OK) return st;
+    if ((st = ensure_weather(ctx, slot)) != MT_OK) return st;
+    MT_CUDA(ctx, mt::launch_generate_weather(
+                     seed32(seed), mt::NoiseOut{ctx->weather[slot], ctx->weather16[0][slot], ctx->weather16[1][slot]},
+                     (cudaStream_t)stream));
+    return MT_OK;
+}
+
+MT_API mt_status mt_download_volumes(mt_ctx* ctx, uint8_t* base, uint8_t* detail, uint8_t* curl, uint8_t* weather,
+                                     int weather_slot) {
+    if (!ctx) return MT_ERR_INVALID_ARG;
+    mt_status st;
+    if ((st = bind_device(ctx)) != MT_OK) return st;
+    MT_CUDA(ctx, cudaDeviceSynchronize());
+    if ((base || detail || curl) && !(ctx->have_base && ctx->have_detail && ctx->have_curl))
+        return fail(ctx, MT_ERR_NO_VOLUMES, "no volumes to download");
+    if (base) MT_CUDA(ctx, cudaMemcpy(base, ctx->base, kBaseTexels * 4, cudaMemcpyDeviceToHost));
+    if (detail) MT_CUDA(ctx, cudaMemcpy(detail, ctx->detail, kDetailTexels * 4, cudaMemcpyDeviceToHost));
+    if (curl) MT_CUDA(ctx, cudaMemcpy(curl, ctx->curl, kCurlTexels * 4, cudaMemcpyDeviceToHost));
+    if (weather) {
+        if (weather_slot < 0 || weather_slot >= MT_MAX_WEATHER_SLOTS || !ctx->weather[weather_slot])
+            return fail(ctx, MT_ERR_NO_VOLUMES, "weather slot %d holds no weather map", weather_slot);
+        MT_CUDA(ctx, cudaMemcpy(weather, ctx->weather[weather_slot], kWeatherTexels * 4, cudaMemcpyDeviceToHost));
+    }
+    return MT_OK;
+}
+
+MT_API mt_status mt_download_volumes_16(mt_ctx* ctx, int storage, uint16_t* base, uint16_t* detail, uint16_t* curl,
+                                        uint16_t* weather, int weather_slot) {
+    if (!ctx) return MT_ERR_INVALID_ARG;
+    if (storage != MT_STORAGE_F16 && storage != MT_STORAGE_BF16)
+        return fail(ctx, MT_ERR_INVALID_ARG, "storage must be MT_STORAGE_F16 or MT_STORAGE_BF16");
+    const int k = storage == MT_STORAGE_F16 ? 0 : 1;
+    mt_status st;
+    if ((st = bind_device(ctx)) != MT_OK) return st;
+    MT_CUDA(ctx, cudaDeviceSynchronize());
+    if ((base || detail || curl) && !(ctx->have_base && ctx->have_detail && ctx->have_curl))
+        return fail(ctx, MT_ERR_NO_VOLUMES, "no volumes to download");
+    if (base) MT_CUDA(ctx, cudaMemcpy(base, ctx->base16[k], kBaseTexels * 8, cudaMemcpyDeviceToHost));
+    if (detail) MT_CUDA(ctx, cudaMemcpy(detail, ctx->detail16[k], kDetailTexels * 8, cudaMemcpyDeviceToHost));
+    if (curl) MT_CUDA(ctx, cudaMemcpy(curl, ctx->curl16[k], kCurlTexels * 8, cudaMemcpyDeviceToHost));
+    if (weather) {
+        if (weather_slot < 0 || weather_slot >= MT_MAX_WEATHER_SLOTS || !ctx->weather[weather_slot])
+            return fail(ctx, MT_ERR_NO_VOLUMES, "weather slot %d holds no weather map", weather_slot);
+        MT_CUDA(ctx, cudaMemcpy(weather, ctx->weather16[k][weather_slot], kWeatherTexels * 8, cudaMemcpyDeviceToHost));
+    }
+    return MT_OK;
+}
+
+MT_API mt_status mt_render(mt_ctx* ctx, const mt_camera_ubo* camera, const mt_camera_ubo* camera_old,
+                           const mt_time_ubo* time, const mt_params* params, const float* prev_rgba, float* cur_rgba,
+                           float* godray_mask, int width, int height, uint32_t flags, void* stream) {
+    if (!ctx) return MT_ERR_INVALID_ARG;
+    mt::MarchArgs a;
+    mt_status st = build_march_args(ctx, camera, camera_old, time, params, prev_rgba, cur_rgba, godray_mask, width,
+                                    height, flags, &a);
+    if (st != MT_OK) return st;
+    if ((st = bind_device(ctx)) != MT_OK) return st;
+    mt::LaunchEvents ev{{ctx->ev[0], ctx->ev[1]}, {ctx->ev[2], ctx->ev[3]}, ctx->timing};
+    MT_CUDA(ctx, mt::launch_render(a, (cudaStream_t)stream, &ev));
+    if (ctx->timing) {
+        ctx->ran[0] = !(flags & MT_RENDER_FULL) || ctx->ran[0];
+        ctx->ran[1] = true;
+    }
+    return MT_OK;
+}
+
+MT_API mt_status mt_txaa(mt_ctx* ctx, const mt_camera_ubo* camera, const mt_camera_ubo* camera_old,
+                         const mt_time_ubo* time, const mt_params* params, const float* current_rgba,
+                         const float* history_rgba, float* out_rgba, int width, int height, void* stream) {
+    if (!ctx) return MT_ERR_INVALID_ARG;
+    if (!camera || !camera_old) return fail(ctx, MT_ERR_INVALID_ARG, "camera and camera_old must not be NULL");
+    mt_status st;
+    if ((st = check_params(ctx, params, time)) != MT_OK) return st;
+    if ((st = check_image(ctx, width, height)) != MT_OK) return st;
+    if (!current_rgba || !history_rgba || !out_rgba)
+        return fail(ctx, MT_ERR_INVALID_ARG, "current, history and out must not be NULL");
+    if (!aligned(current_rgba, 16) || !aligned(history_rgba, 16) || !aligned(out_rgba, 16))
+        return fail(ctx, MT_ERR_INVALID_ARG, "images must be 16-byte aligned");
+    if (out_rgba == current_rgba || out_rgba == history_rgba)
+        return fail(ctx, MT_ERR_INVALID_ARG, "out_rgba must differ from current_rgba and history_rgba");
+    if ((st = bind_device(ctx)) != MT_OK) return st;
+    mt::TxaaArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.camera = *camera;
+    a.camera_old = *camera_old;
+    a.time = *time;
+    a.params = *params;
+    a.current = (const float4*)current_rgba;
+    a.history = (const float4*)history_rgba;
+    a.out = (float4*)out_rgba;
+    a.width = width;
+    a.height = height;
+    MT_CUDA(ctx, mt::launch_txaa(a, (cudaStream_t)stream, ctx->timing ? &ctx->ev[4] : nullptr));
+    if (ctx->timing) ctx->ran[2] = true;
+    return MT_OK;
+}
+
+MT_API mt_status mt_render_batch(mt_ctx* ctx, const mt_view* views, int n_views, void* stream) {
+    if (!ctx) return MT_ERR_INVALID_ARG;
+    if (n_views < 0 || (n_views > 0 && !views)) return fail(ctx, MT_ERR_INVALID_ARG, "bad view list");
+    for (int i = 0; i < n_views; ++i) {
+        const mt_view& v = views[i];
+        mt_status st = mt_render(ctx, &v.camera, &v.camera_old, &v.time, &v.params, v.prev_rgba, v.cur_rgba,
+                                 v.godray_mask, v.width, v.height, v.flags, stream);
+        if (st != MT_OK) return st;
+    }
+    return MT_OK;
+}
+
+MT_API mt_status mt_get_stats(mt_ctx* ctx, mt_stats* out, int reset, void* stream) {
+    if (!ctx) return MT_ERR_INVALID_ARG;
+    if (!out) return fail(ctx, MT_ERR_INVALID_ARG, "out must not be NULL");
+    mt_status st;
+    if ((st = bind_device(ctx)) != MT_OK) return st;
+    MT_CUDA(ctx, cudaStreamSynchronize((cudaStream_t)stream));
+    unsigned long long h[4];
+    MT_CUDA(ctx, cudaMemcpy(h, ctx->stats, sizeof(h), cudaMemcpyDeviceToHost));
+    out->primary_samples = h[0];
+    out->light_samples = h[1];
+    out->marched_rays = h[2];
+    out->pixels = h[3];
+    if (reset) MT_CUDA(ctx, cudaMemset(ctx->stats, 0, sizeof(h)));
+    return MT_OK;
+}
+
+MT_API mt_status mt_set_timing(mt_ctx* ctx, int enabled) {
+    if (!ctx) return MT_ERR_INVALID_ARG;
+    mt_status st;
+    if ((st = bind_device(ctx)) != MT_OK) return st;
+    if (enabled && !ctx->ev[0])
+        for (cudaEvent_t& e : ctx->ev) MT_CUDA(ctx, cudaEventCreate(&e));
+    ctx->timing = enabled != 0;
+    ctx->ran[0] = ctx->ran[1] = ctx->ran[2] = false;
+    return MT_OK;
+}
+
+MT_API mt_status mt_get_kernel_times(mt_ctx* ctx, mt_kernel_times* out) {
+    if (!ctx) return MT_ERR_INVALID_ARG;
+    if (!out) return fail(ctx, MT_ERR_INVALID_ARG, "out must not be NULL");
+    std::memset(out, 0, sizeof(*out));
+    if (!ctx->ev[0]) return MT_OK;
+    mt_status st;
+    if ((st = bind_device(ctx)) != MT_OK) return st;
+    float* dst[3] = {&out->reproject_ms, &out->march_ms, &out->txaa_ms};
+    for (int k = 0; k < 3; ++k) {
+        if (!ctx->ran[k]) continue;
+        MT_CUDA(ctx, cudaEventSynchronize(ctx->ev[2 * k + 1]));
+        MT_CUDA(ctx, cudaEventElapsedTime(dst[k], ctx->ev[2 * k], ctx->ev[2 * k + 1]));
+    }
+    return MT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,147 @@
+// Device-side arithmetic of the compute stage, GLSL semantics, FP32.
+//
+// The translation units that include this header are compiled with
+// -fmad=false and IEEE division/square root, and every expression below keeps
+// the operation order of the reference shaders, so the control flow of the
+// march (the `t += stepSize` recurrence, the `baseDensity > 0` branch and the
+// `accumDensity >= 1` exit of cloudRayMarch.comp:627-684) is reproduced exactly.
+// Only exp/pow/acos/cos (CUDA's libdevice vs the host's libm) may differ in
+// the last bits, and they feed colour only, never control flow.
+//
+// Fixed meanings of what GLSL leaves to the implementation:
+//   dot = ((a.x*b.x + a.y*b.y) + a.z*b.z); normalize(v) = v / length(v);
+//   mix(x,y,a) = x*(1-a) + y*a; min(x,y) = y<x ? y : x; max(x,y) = x<y ? y : x;
+//   round = half away from zero; float->int truncates and saturates (NaN -> 0).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/meteoros.h"
+
+#define MT_HD __device__ __forceinline__
+
+namespace mt {
+
+struct f3 {
+    float x, y, z;
+};
+struct f4v {
+    float x, y, z, w;
+};
+
+MT_HD f3 mk3(float x, float y, float z) { return f3{x, y, z}; }
+MT_HD f3 operator+(f3 a, f3 b) { return f3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+MT_HD f3 operator-(f3 a, f3 b) { return f3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+MT_HD f3 operator-(f3 a) { return f3{-a.x, -a.y, -a.z}; }
+MT_HD f3 operator*(f3 a, f3 b) { return f3{a.x * b.x, a.y * b.y, a.z * b.z}; }
+MT_HD f3 operator*(f3 a, float s) { return f3{a.x * s, a.y * s, a.z * s}; }
+MT_HD f3 operator*(float s, f3 a) { return f3{s * a.x, s * a.y, s * a.z}; }
+MT_HD f3 operator/(f3 a, float s) { return f3{a.x / s, a.y / s, a.z / s}; }
+MT_HD f3 operator/(f3 a, f3 b) { return f3{a.x / b.x, a.y / b.y, a.z / b.z}; }
+MT_HD f4v operator+(f4v a, f4v b) { return f4v{a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w}; }
+MT_HD f4v operator-(f4v a, f4v b) { return f4v{a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w}; }
+MT_HD f4v operator*(f4v a, float s) { return f4v{a.x * s, a.y * s, a.z * s, a.w * s}; }
+MT_HD f4v operator/(f4v a, float s) { return f4v{a.x / s, a.y / s, a.z / s, a.w / s}; }
+
+MT_HD float gmin(float a, float b) { return b < a ? b : a; }
+MT_HD float gmax(float a, float b) { return a < b ? b : a; }
+MT_HD int imin(int a, int b) { return b < a ? b : a; }
+MT_HD int imax(int a, int b) { return a < b ? b : a; }
+MT_HD float gclamp(float x, float lo, float hi) { return gmin(gmax(x, lo), hi); }
+MT_HD float gmix(float x, float y, float a) { return x * (1.0f - a) + y * a; }
+MT_HD float gfract(float x) { return x - floorf(x); }
+MT_HD float gmod(float x, float y) { return x - y * floorf(x / y); }
+MT_HD float gsmoothstep(float e0, float e1, float x) {
+    float t = gclamp((x - e0) / (e1 - e0), 0.0f, 1.0f);
+    return t * t * (3.0f - 2.0f * t);
+}
+// cvt.rzi.s32.f32: truncation, saturating to the int range, NaN -> 0.
+MT_HD int f2i(float v) { return __float2int_rz(v); }
+
+MT_HD float dot3(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+MT_HD float length3(f3 a) { return sqrtf(dot3(a, a)); }
+MT_HD f3 normalize3(f3 a) { return a / length3(a); }
+MT_HD f3 cross3(f3 a, f3 b) { return f3{a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y}; }
+MT_HD f3 mix3(f3 x, f3 y, float a) { return f3{gmix(x.x, y.x, a), gmix(x.y, y.y, a), gmix(x.z, y.z, a)}; }
+MT_HD f4v min4(f4v a, f4v b) { return f4v{gmin(a.x, b.x), gmin(a.y, b.y), gmin(a.z, b.z), gmin(a.w, b.w)}; }
+MT_HD f4v max4(f4v a, f4v b) { return f4v{gmax(a.x, b.x), gmax(a.y, b.y), gmax(a.z, b.z), gmax(a.w, b.w)}; }
+MT_HD f4v mix4(f4v x, f4v y, float a) { return f4v{gmix(x.x, y.x, a), gmix(x.y, y.y, a), gmix(x.z, y.z, a), gmix(x.w, y.w, a)}; }
+MT_HD f3 ld3(const float* p) { return f3{p[0], p[1], p[2]}; }
+
+// GLSL mat3(c0,c1,c2) * v
+MT_HD f3 mat3mul(f3 c0, f3 c1, f3 c2, f3 v) {
+    return f3{c0.x * v.x + c1.x * v.y + c2.x * v.z, c0.y * v.x + c1.y * v.y + c2.y * v.z,
+              c0.z * v.x + c1.z * v.y + c2.z * v.z};
+}
+
+MT_HD float lerp1(float p, float q, float t) { return p + t * (q - p); }
+MT_HD f4v lerp4(f4v p, f4v q, float t) {
+    return f4v{lerp1(p.x, q.x, t), lerp1(p.y, q.y, t), lerp1(p.z, q.z, t), lerp1(p.w, q.w, t)};
+}
+
+MT_HD f4v unpack_rgba8(uint32_t v) {
+    return f4v{(float)(v & 0xffu), (float)((v >> 8) & 0xffu), (float)((v >> 16) & 0xffu), (float)(v >> 24)};
+}
+
+// ---------------------------------------------------------------------------
+// Samplers.  Vulkan LINEAR filter with exact FP32 weights: u = s*N - 0.5,
+// i0 = floor(u), alpha = u - i0, REPEAT wraps the integer texel coordinate
+// (N is a power of two).  Raw texel values are interpolated x, then y, then
+// z, and the result is scaled once (1/255 for UNORM8).  The volumes are
+// RGBA8 words, x fastest, then y, then z (ImageLoadingUtility.cpp:75-139).
+// ---------------------------------------------------------------------------
+template <int N> MT_HD f4v tex3_u8(const uint32_t* __restrict__ vol, f3 s) {
+    constexpr unsigned M = (unsigned)N - 1u;
+    const float fn = (float)N;
+    float u = s.x * fn - 0.5f, v = s.y * fn - 0.5f, w = s.z * fn - 0.5f;
+    float fu = floorf(u), fv = floorf(v), fw = floorf(w);
+    float a = u - fu, b = v - fv, g = w - fw;
+    unsigned iu = (unsigned)f2i(fu), iv = (unsigned)f2i(fv), iw = (unsigned)f2i(fw);
+    unsigned x0 = iu & M, x1 = (iu + 1u) & M, y0 = iv & M, y1 = (iv + 1u) & M, z0 = iw & M, z1 = (iw + 1u) & M;
+    const uint32_t* p0 = vol + (size_t)z0 * (N * N);
+    const uint32_t* p1 = vol + (size_t)z1 * (N * N);
+    uint32_t t000 = __ldg(p0 + y0 * N + x0), t100 = __ldg(p0 + y0 * N + x1);
+    uint32_t t010 = __ldg(p0 + y1 * N + x0), t110 = __ldg(p0 + y1 * N + x1);
+    uint32_t t001 = __ldg(p1 + y0 * N + x0), t101 = __ldg(p1 + y0 * N + x1);
+    uint32_t t011 = __ldg(p1 + y1 * N + x0), t111 = __ldg(p1 + y1 * N + x1);
+    f4v c00 = lerp4(unpack_rgba8(t000), unpack_rgba8(t100), a);
+    f4v c10 = lerp4(unpack_rgba8(t010), unpack_rgba8(t110), a);
+    f4v c01 = lerp4(unpack_rgba8(t001), unpack_rgba8(t101), a);
+    f4v c11 = lerp4(unpack_rgba8(t011), unpack_rgba8(t111), a);
+    f4v c0 = lerp4(c00, c10, b);
+    f4v c1 = lerp4(c01, c11, b);
+    return lerp4(c0, c1, g) * (1.0f / 255.0f);
+}
+
+template <int N> MT_HD f4v tex2_u8(const uint32_t* __restrict__ img, float sx, float sy) {
+    constexpr unsigned M = (unsigned)N - 1u;
+    const float fn = (float)N;
+    float u = sx * fn - 0.5f, v = sy * fn - 0.5f;
+    float fu = floorf(u), fv = floorf(v);
+    float a = u - fu, b = v - fv;
+    unsigned iu = (unsigned)f2i(fu), iv = (unsigned)f2i(fv);
+    unsigned x0 = iu & M, x1 = (iu + 1u) & M, y0 = iv & M, y1 = (iv + 1u) & M;
+    f4v c0 = lerp4(unpack_rgba8(__ldg(img + y0 * N + x0)), unpack_rgba8(__ldg(img + y0 * N + x1)), a);
+    f4v c1 = lerp4(unpack_rgba8(__ldg(img + y1 * N + x0)), unpack_rgba8(__ldg(img + y1 * N + x1)), a);
+    return lerp4(c0, c1, b) * (1.0f / 255.0f);
+}
+
+// Bilinear sample of an RGBA32F frame with CLAMP_TO_BORDER, opaque black
+// border (Texture2D.cpp:75 with Image.cpp:324).
+MT_HD f4v tex2_border(const float4* __restrict__ img, int W, int H, float sx, float sy) {
+    float u = sx * (float)W - 0.5f, v = sy * (float)H - 0.5f;
+    float fu = floorf(u), fv = floorf(v);
+    float a = u - fu, b = v - fv;
+    int i0 = f2i(fu), j0 = f2i(fv);
+    long long i1 = (long long)i0 + 1, j1 = (long long)j0 + 1;
+    auto at = [&](long long i, long long j) -> f4v {
+        if (i < 0 || j < 0 || i >= W || j >= H) return f4v{0.0f, 0.0f, 0.0f, 1.0f};
+        float4 q = __ldg(img + (size_t)j * (size_t)W + (size_t)i);
+        return f4v{q.x, q.y, q.z, q.w};
+    };
+    f4v c0 = lerp4(at(i0, j0), at(i1, j0), a);
+    f4v c1 = lerp4(at(i0, j1), at(i1, j1), a);
+    return lerp4(c0, c1, b);
+}
+
+}  // namespace mt

@@ -1,0 +1,68 @@
+// Kernel argument blocks and launchers shared by the C ABI (mt_capi.cu) and
+// the kernel translation units.  Arguments travel by value as
+// __grid_constant__ parameters: the uniform blocks of the reference
+// (CameraUBO, TimeUBO) plus mt_params fit easily in the parameter space.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/meteoros.h"
+
+namespace mt {
+
+struct MarchArgs {
+    mt_camera_ubo camera;
+    mt_camera_ubo camera_old;
+    mt_time_ubo time;
+    mt_params params;
+    const uint32_t* base;     // MT_BASE_N^3 RGBA8 words
+    const uint32_t* detail;   // MT_DETAIL_N^3 RGBA8 words
+    const uint32_t* curl;     // MT_CURL_N^2 RGBA8 words
+    const uint32_t* weather;  // MT_WEATHER_N^2 RGBA8 words (slot params.weather_slot)
+    const float4* prev;
+    float4* cur;
+    float* mask;
+    unsigned long long* stats;  // 4 counters or NULL
+    int32_t width, height;
+    int32_t groups_x, groups_y;  // 4x4 blocks covered by the reference's raymarch dispatch
+    uint32_t flags;
+};
+
+struct TxaaArgs {
+    mt_camera_ubo camera;
+    mt_camera_ubo camera_old;
+    mt_time_ubo time;
+    mt_params params;
+    const float4* current;
+    const float4* history;
+    float4* out;
+    int32_t width, height;
+};
+
+// Outputs of one generator launch (any pointer may be NULL).
+struct NoiseOut {
+    uint32_t* u8;   // RGBA8 words
+    uint2* h16;     // 4 x IEEE half per texel
+    uint2* b16;     // 4 x bfloat16 per texel
+};
+
+// Optional event pairs bracketing each launch (NULL: no timing).
+struct LaunchEvents {
+    cudaEvent_t reproject[2];
+    cudaEvent_t march[2];
+    bool on;
+};
+
+cudaError_t launch_render(const MarchArgs& a, cudaStream_t s, const LaunchEvents* ev);
+cudaError_t launch_txaa(const TxaaArgs& a, cudaStream_t s, const cudaEvent_t* ev);
+cudaError_t launch_generate_base(uint32_t seed, NoiseOut o, cudaStream_t s);
+cudaError_t launch_generate_detail(uint32_t seed, NoiseOut o, cudaStream_t s);
+cudaError_t launch_generate_curl(uint32_t seed, NoiseOut o, cudaStream_t s);
+cudaError_t launch_generate_weather(uint32_t seed, NoiseOut o, cudaStream_t s);
+cudaError_t launch_u8_to_16(const uint32_t* src, size_t n, uint2* h16, uint2* b16, cudaStream_t s);
+
+// Number of 4x4 blocks along one axis covered by the reference's raymarch
+// dispatch: ceil(floor(dim/4) / 32) groups of 32 (Renderer.cpp:713-716).
+inline int march_groups(int dim) { return 32 * ((dim / 4 + 31) / 32); }
+
+}  // namespace mt

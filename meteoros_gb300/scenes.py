@@ -1,0 +1,93 @@
+"""Seeded scene builders: the uniform blocks of the benchmark configurations.
+
+The reference drives its uniforms from an interactive window (main.cpp:172-186:
+keyboard-rotated camera, wall-clock time); these builders produce the same
+uniform blocks deterministically from a seed:
+
+  reference_frame   the reference's own camera (main.cpp:157-160: eye (0,0,2)
+                    looking toward (0,0,1), fovy 45 deg) with optional pitch
+  config_view       a camera at 100 m altitude, FOV 60 deg, yaw in [0,360),
+                    pitch in [5,30] deg, sun uniform on the upper hemisphere,
+                    wind 10 m/s at heading 45 deg (mt_params_config)
+  config_sequence   16 frames yawing 0.5 deg/frame with t += 0.16 s/frame
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import abi
+
+
+def _forward(yaw_deg: float, pitch_deg: float):
+    y, p = math.radians(yaw_deg), math.radians(pitch_deg)
+    return (math.cos(p) * math.sin(y), math.sin(p), -math.cos(p) * math.cos(y))
+
+
+def look(eye, yaw_deg: float, pitch_deg: float, fovy_deg: float, width: int, height: int) -> abi.CameraUBO:
+    f = _forward(yaw_deg, pitch_deg)
+    ref = tuple(e + d for e, d in zip(eye, f))
+    return abi.camera_look_at(eye, ref, fovy_deg, width / height, 0.1, 1000.0)
+
+
+def sun_direction(rng: np.random.Generator):
+    """Uniform on the upper hemisphere (y up)."""
+    y = float(rng.uniform(0.0, 1.0))
+    phi = float(rng.uniform(0.0, 2.0 * math.pi))
+    r = math.sqrt(max(0.0, 1.0 - y * y))
+    return (r * math.cos(phi), y, r * math.sin(phi))
+
+
+def set_sun(params: abi.Params, direction, distance: float = 1.0e9) -> abi.Params:
+    for i in range(3):
+        params.sun_light_pos[i] = direction[i] * distance
+        params.sky_sun_pos[i] = direction[i] * distance
+    return params
+
+
+def reference_frame(width: int, height: int, pitch_deg: float = 0.0, frame: int = 0, t: float = 0.0):
+    """The reference's camera and constants (REF preset)."""
+    cam = look((0.0, 0.0, 2.0), 0.0, pitch_deg, 45.0, width, height)
+    tm = abi.time_init()
+    tm.frame_count_mod16 = frame % 16
+    tm.time[1] = t
+    return cam, tm, abi.params_reference()
+
+
+def config_view(seed: int, width: int, height: int, steps: int | None = None):
+    """Camera, time and params of one benchmark view (configs 0, 2, 3)."""
+    rng = np.random.default_rng(seed)
+    yaw = float(rng.uniform(0.0, 360.0))
+    pitch = float(rng.uniform(5.0, 30.0))
+    cam = look((0.0, 100.0, 0.0), yaw, pitch, 60.0, width, height)
+    params = set_sun(abi.params_config(), sun_direction(rng))
+    if steps is not None:
+        params.steps_min = params.steps_max = int(steps)
+    tm = abi.time_init()
+    return cam, tm, params, (yaw, pitch)
+
+
+def config_sequence(seed: int, width: int, height: int, frames: int = 16, yaw_step: float = 0.5,
+                    dt: float = 0.16):
+    """Per-frame (camera, camera_old, time, params) of the reprojected sequence (config 1)."""
+    cam0, tm, params, (yaw, pitch) = config_view(seed, width, height)
+    out = []
+    old = cam0
+    for i in range(frames):
+        cam = look((0.0, 100.0, 0.0), yaw + yaw_step * i, pitch, 60.0, width, height)
+        t = abi.TimeUBO()
+        C_copy(t, tm)
+        t.frame_count_mod16 = i % 16
+        t.time[0] = dt if i > 0 else 0.0
+        t.time[1] = dt * i
+        out.append((cam, old, t, params))
+        old = cam
+    return out
+
+
+def C_copy(dst, src):
+    import ctypes
+
+    ctypes.memmove(ctypes.addressof(dst), ctypes.addressof(src), ctypes.sizeof(src))
+    return dst

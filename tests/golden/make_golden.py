@@ -1,0 +1,123 @@
+"""Make tests/golden/golden.npz from the reference's own shader source.
+
+The reference has no tests, fixtures or golden images.  The golden vectors
+here are produced by running its GLSL shaders -- compiled as C++ by
+oracle/ref_build.py from the reference tree -- on seeded synthetic inputs:
+
+  repro_f{k}, mask_f{k}   cloudRayMarch.comp + reprojection.comp, REF constants,
+                          a 64x36 16-frame checkerboard sequence starting from a
+                          seeded random previous frame (k = 0, 7, 15 kept)
+  quirk_rgba, quirk_mask  a 130x18 frame: floor(130/4) = 32 blocks is a whole
+                          number of 32-wide groups, so the reference's dispatch
+                          (Renderer.cpp:713-716) never marches columns 128-129
+  txaa_out                postProcess_TXAA.frag on seeded current/history images
+  wang_uvs, wang_val      WangHashNoise (postProcess_ToneMap.frag:52-66)
+  gen_sha256_*            SHA-256 of the seed-7 generator volumes (pins the
+                          generator bit for bit across hosts)
+
+The noise volumes fed to the shaders come from the seed-7 generator, with
+the base shape's R channel scaled by 0.8 (`golden_volumes`): under the
+reference's constants the unscaled volume gives a fully overcast sky, where
+every ray saturates and the god-ray mask is identically zero.  The run
+needs the reference tree (METEOROS_REFERENCE, default /root/reference); the
+tests only read the .npz.
+
+Usage: python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import hashlib
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+from meteoros_gb300 import abi, build, scenes  # noqa: E402
+from oracle import pyoracle, pyref  # noqa: E402
+
+OUT = Path(__file__).resolve().parent / "golden.npz"
+
+SEQ_W, SEQ_H, SEQ_PITCH = 64, 36, 20.0
+QUIRK_W, QUIRK_H, QUIRK_FRAME = 130, 18, 5
+KEEP = (0, 7, 15)
+
+
+def sequence_inputs():
+    """Cameras and times of the 16-frame REF sequence (camera yaws 0.25 deg/frame)."""
+    frames = []
+    old = scenes.look((0.0, 0.0, 2.0), 0.0, SEQ_PITCH, 45.0, SEQ_W, SEQ_H)
+    for f in range(16):
+        cam = scenes.look((0.0, 0.0, 2.0), 0.25 * f, SEQ_PITCH, 45.0, SEQ_W, SEQ_H)
+        tm = abi.time_init()
+        tm.frame_count_mod16 = f
+        tm.time[0] = 0.016
+        tm.time[1] = 0.016 * f
+        frames.append((cam, old, tm))
+        old = cam
+    return frames
+
+
+def golden_volumes(v: dict) -> pyoracle.Volumes:
+    base = v["base"].copy()
+    base[..., 0] = np.floor(base[..., 0].astype(np.float32) * 0.8).astype(np.uint8)
+    return pyoracle.Volumes(base, v["detail"], v["curl"], v["weather"])
+
+
+def initial_prev():
+    return np.random.default_rng(0).random((SEQ_H, SEQ_W, 4), dtype=np.float32)
+
+
+def txaa_inputs():
+    rng = np.random.default_rng(1)
+    cur = (rng.random((SEQ_H, SEQ_W, 4), dtype=np.float32) * 2.0).astype(np.float32)
+    hist = (rng.random((SEQ_H, SEQ_W, 4), dtype=np.float32) * 2.0).astype(np.float32)
+    old = scenes.look((0.0, 0.0, 2.0), 0.0, SEQ_PITCH, 45.0, SEQ_W, SEQ_H)
+    cam = scenes.look((0.0, 0.0, 2.0), 0.5, SEQ_PITCH + 0.3, 45.0, SEQ_W, SEQ_H)
+    tm = abi.time_init()
+    tm.frame_count_mod16 = 9
+    return cam, old, tm, cur, hist
+
+
+def wang_inputs():
+    return np.random.default_rng(2).integers(0, 2**32, size=(256, 3), dtype=np.uint64).astype(np.uint32)
+
+
+def main() -> int:
+    build.build()
+    if not pyref.available():
+        print("reference tree not found: cannot make golden vectors")
+        return 1
+    v = pyoracle.generate_volumes(7)
+    vol = golden_volumes(v)
+    out = {}
+    prev = initial_prev()
+    for f, (cam, old, tm) in enumerate(sequence_inputs()):
+        rgba, mask = pyref.frame(vol, cam, old, tm, prev, SEQ_W, SEQ_H)
+        if f in KEEP:
+            out[f"repro_f{f}"] = rgba
+            out[f"mask_f{f}"] = mask
+        prev = rgba
+    cam = scenes.look((0.0, 0.0, 2.0), 0.0, SEQ_PITCH, 45.0, QUIRK_W, QUIRK_H)
+    tm = abi.time_init()
+    tm.frame_count_mod16 = QUIRK_FRAME
+    qprev = np.random.default_rng(3).random((QUIRK_H, QUIRK_W, 4), dtype=np.float32)
+    out["quirk_rgba"], out["quirk_mask"] = pyref.frame(vol, cam, cam, tm, qprev, QUIRK_W, QUIRK_H)
+    cam, old, tm, cur, hist = txaa_inputs()
+    out["txaa_out"] = pyref.txaa(cam, old, tm, cur, hist)
+    uvs = wang_inputs()
+    out["wang_uvs"] = uvs
+    out["wang_val"] = np.array([pyref.wang_hash_noise(int(a), int(b), int(c)) for a, b, c in uvs], np.float32)
+    for k in ("base", "detail", "curl", "weather"):
+        for suffix in ("", "_h16", "_b16"):
+            out[f"gen_sha256_{k}{suffix}"] = np.frombuffer(
+                hashlib.sha256(np.ascontiguousarray(v[k + suffix]).tobytes()).digest(), np.uint8)
+    np.savez_compressed(OUT, **out)
+    print(f"wrote {OUT} ({OUT.stat().st_size} bytes)")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

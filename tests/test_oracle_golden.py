@@ -1,0 +1,114 @@
+"""The oracle (CPU restatement) against the golden vectors produced by the
+reference's own shader source, and -- where the reference tree is present --
+against that source directly.  CPU only."""
+import numpy as np
+import pytest
+
+from meteoros_gb300 import abi
+from tests.golden import make_golden as mg
+
+
+def bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.uint32)
+
+
+def assert_bit_exact(a, b, what):
+    a, b = np.asarray(a, np.float32), np.asarray(b, np.float32)
+    assert a.shape == b.shape, what
+    nan_a, nan_b = np.isnan(a), np.isnan(b)
+    assert np.array_equal(nan_a, nan_b), f"{what}: written-pixel pattern differs"
+    diff = bits(np.where(nan_a, 0, a)) != bits(np.where(nan_b, 0, b))
+    assert not diff.any(), f"{what}: {int(diff.sum())} values differ, max {np.nanmax(np.abs(a - b))}"
+
+
+def test_sequence_matches_golden(oracle, volumes_seed7, golden, lib):
+    vol = mg.golden_volumes(volumes_seed7)
+    params = abi.params_reference()
+    prev = mg.initial_prev()
+    for f, (cam, old, tm) in enumerate(mg.sequence_inputs()):
+        rgba, mask, _ = oracle.render(vol, cam, old, tm, params, prev, mg.SEQ_W, mg.SEQ_H,
+                                      abi.MT_RENDER_CHECKERBOARD)
+        if f in mg.KEEP:
+            assert_bit_exact(rgba, golden[f"repro_f{f}"], f"frame {f} rgba")
+            assert_bit_exact(mask, golden[f"mask_f{f}"], f"frame {f} mask")
+        prev = rgba
+
+
+def test_dispatch_quirk_matches_golden(oracle, volumes_seed7, golden, lib):
+    vol = mg.golden_volumes(volumes_seed7)
+    cam = mg.scenes.look((0.0, 0.0, 2.0), 0.0, mg.SEQ_PITCH, 45.0, mg.QUIRK_W, mg.QUIRK_H)
+    tm = abi.time_init()
+    tm.frame_count_mod16 = mg.QUIRK_FRAME
+    prev = np.random.default_rng(3).random((mg.QUIRK_H, mg.QUIRK_W, 4), dtype=np.float32)
+    rgba, mask, _ = oracle.render(vol, cam, cam, tm, abi.params_reference(), prev, mg.QUIRK_W, mg.QUIRK_H, 0)
+    assert_bit_exact(rgba, golden["quirk_rgba"], "quirk rgba")
+    assert_bit_exact(mask, golden["quirk_mask"], "quirk mask")
+    # columns 128 and 129 are never marched by the reference's dispatch
+    assert np.isnan(mask[:, 128:]).all()
+
+
+def test_txaa_matches_golden(oracle, golden, lib):
+    cam, old, tm, cur, hist = mg.txaa_inputs()
+    out = oracle.txaa(cam, old, tm, abi.params_reference(), cur, hist)
+    assert_bit_exact(out, golden["txaa_out"], "txaa")
+
+
+def test_wang_hash_matches_reference(oracle, golden):
+    uvs = golden["wang_uvs"]
+    h = np.array([oracle.lib().orc_wang(int(a), int(b), int(c)) for a, b, c in uvs], np.uint32)
+    # WangHashNoise returns float(seed) * (1.0 / 4294967296.0) in float32
+    val = h.astype(np.float32) * np.float32(1.0 / 4294967296.0)
+    assert_bit_exact(val, golden["wang_val"], "WangHashNoise")
+
+
+def test_generator_matches_golden_hashes(volumes_seed7, golden):
+    import hashlib
+
+    for k in ("base", "detail", "curl", "weather"):
+        for suffix in ("", "_h16", "_b16"):
+            digest = hashlib.sha256(np.ascontiguousarray(volumes_seed7[k + suffix]).tobytes()).digest()
+            assert digest == golden[f"gen_sha256_{k}{suffix}"].tobytes(), f"{k}{suffix}"
+
+
+# ---- directly against the reference's shader source (needs the reference tree) ----
+
+@pytest.fixture(scope="module")
+def pyref():
+    from oracle import pyref
+
+    if not pyref.available():
+        pytest.skip("reference tree not present")
+    return pyref
+
+
+@pytest.mark.parametrize("size", [(48, 28), (67, 41)])
+def test_every_frame_slot_matches_reference_source(oracle, pyref, volumes_seed7, lib, size):
+    w, h = size
+    vol = mg.golden_volumes(volumes_seed7)
+    rng = np.random.default_rng(w)
+    prev = rng.random((h, w, 4), dtype=np.float32) * 3.0
+    old = mg.scenes.look((0.0, 0.0, 2.0), 3.0, 14.0, 45.0, w, h)
+    cam = mg.scenes.look((0.0, 0.0, 2.0), 4.0, 15.0, 45.0, w, h)
+    for f in range(16):
+        tm = abi.time_init()
+        tm.frame_count_mod16 = f
+        tm.time[1] = 1.7 * f
+        a, am, _ = oracle.render(vol, cam, old, tm, abi.params_reference(), prev, w, h, 0)
+        b, bm = pyref.frame(vol, cam, old, tm, prev, w, h)
+        assert_bit_exact(a, b, f"frame slot {f} rgba")
+        assert_bit_exact(am, bm, f"frame slot {f} mask")
+
+
+def test_txaa_matches_reference_source(oracle, pyref, lib):
+    rng = np.random.default_rng(11)
+    w, h = 57, 33
+    cur = rng.random((h, w, 4), dtype=np.float32) * 5.0
+    hist = rng.random((h, w, 4), dtype=np.float32) * 5.0
+    old = mg.scenes.look((0.0, 0.0, 2.0), 0.0, 10.0, 45.0, w, h)
+    cam = mg.scenes.look((0.0, 0.0, 2.0), 2.0, 11.0, 45.0, w, h)
+    for f in (0, 5, 13):
+        tm = abi.time_init()
+        tm.frame_count_mod16 = f
+        a = oracle.txaa(cam, old, tm, abi.params_reference(), cur, hist)
+        b = pyref.txaa(cam, old, tm, cur, hist)
+        assert_bit_exact(a, b, f"txaa slot {f}")
