@@ -623,8 +623,10 @@ cudaError_t launch_render(const MarchArgs& a, cudaStream_t s, const LaunchEvents
     }
     const long long m = (a.flags & MT_RENDER_FULL) ? (long long)a.width * a.height
                                                    : (long long)a.groups_x * a.groups_y;
+    // Images narrower or shorter than 4 pixels give the reference an empty
+    // raymarch dispatch (Renderer.cpp:713-716): nothing is marched.
     if (timed) cudaEventRecord(ev->march[0], s);
-    march_kernel<<<(unsigned)((m + 127) / 128), 128, 0, s>>>(a);
+    if (m > 0) march_kernel<<<(unsigned)((m + 127) / 128), 128, 0, s>>>(a);
     if (timed) cudaEventRecord(ev->march[1], s);
     return cudaGetLastError();
 }

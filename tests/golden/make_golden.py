@@ -14,6 +14,12 @@ oracle/ref_build.py from the reference tree -- on seeded synthetic inputs:
   wang_uvs, wang_val      WangHashNoise (postProcess_ToneMap.frag:52-66)
   gen_sha256_*            SHA-256 of the seed-7 generator volumes (pins the
                           generator bit for bit across hosts)
+  *_ubo                   the exact uniform-block bytes every golden was made
+                          with: cameras are built with tan/sin/cos of the host's
+                          libm, which may differ by an ulp between hosts, and an
+                          ulp in a ray direction can move a density-threshold
+                          crossing; tests read these bytes instead of
+                          rebuilding the uniforms
 
 The noise volumes fed to the shaders come from the seed-7 generator, with
 the base shape's R channel scaled by 0.8 (`golden_volumes`): under the
@@ -60,6 +66,31 @@ def sequence_inputs():
     return frames
 
 
+def ubo_bytes(*structs) -> np.ndarray:
+    import ctypes
+
+    return np.frombuffer(b"".join(ctypes.string_at(ctypes.addressof(x), ctypes.sizeof(x)) for x in structs),
+                         np.uint8).copy()
+
+
+def ubos_from(blob: np.ndarray, *types):
+    out, off = [], 0
+    raw = bytes(np.asarray(blob, np.uint8))
+    for t in types:
+        import ctypes
+
+        n = ctypes.sizeof(t)
+        out.append(t.from_buffer_copy(raw[off:off + n]))
+        off += n
+    return out
+
+
+def golden_sequence(golden: dict):
+    """The 16 (camera, camera_old, time) triples the sequence golden was made with."""
+    return [tuple(ubos_from(golden[f"seq_ubo_f{f}"], abi.CameraUBO, abi.CameraUBO, abi.TimeUBO))
+            for f in range(16)]
+
+
 def golden_volumes(v: dict) -> pyoracle.Volumes:
     base = v["base"].copy()
     base[..., 0] = np.floor(base[..., 0].astype(np.float32) * 0.8).astype(np.uint8)
@@ -95,6 +126,7 @@ def main() -> int:
     out = {}
     prev = initial_prev()
     for f, (cam, old, tm) in enumerate(sequence_inputs()):
+        out[f"seq_ubo_f{f}"] = ubo_bytes(cam, old, tm)
         rgba, mask = pyref.frame(vol, cam, old, tm, prev, SEQ_W, SEQ_H)
         if f in KEEP:
             out[f"repro_f{f}"] = rgba
@@ -104,8 +136,10 @@ def main() -> int:
     tm = abi.time_init()
     tm.frame_count_mod16 = QUIRK_FRAME
     qprev = np.random.default_rng(3).random((QUIRK_H, QUIRK_W, 4), dtype=np.float32)
+    out["quirk_ubo"] = ubo_bytes(cam, tm)
     out["quirk_rgba"], out["quirk_mask"] = pyref.frame(vol, cam, cam, tm, qprev, QUIRK_W, QUIRK_H)
     cam, old, tm, cur, hist = txaa_inputs()
+    out["txaa_ubo"] = ubo_bytes(cam, old, tm)
     out["txaa_out"] = pyref.txaa(cam, old, tm, cur, hist)
     uvs = wang_inputs()
     out["wang_uvs"] = uvs

@@ -83,12 +83,12 @@ def ref_ctx(lib, volumes_seed7):
     c.close()
 
 
-def test_reference_sequence_each_frame(ref_ctx, oracle):
+def test_reference_sequence_each_frame(ref_ctx, oracle, golden):
     """16 checkerboard frames, REF constants: each frame from the same previous image."""
     ctx, vol = ref_ctx
     params = abi.params_reference()
     prev = mg.initial_prev()
-    for f, (cam, old, tm) in enumerate(mg.sequence_inputs()):
+    for f, (cam, old, tm) in enumerate(mg.golden_sequence(golden)):
         a, _, _ = oracle.render(vol, cam, old, tm, params, prev, mg.SEQ_W, mg.SEQ_H, 0)
         check_frame(oracle, vol, ctx, cam, old, tm, params, prev, mg.SEQ_W, mg.SEQ_H, 0, f"frame {f}")
         prev = a
@@ -99,7 +99,7 @@ def test_reference_sequence_against_golden(ref_ctx, golden):
     ctx, vol = ref_ctx
     params = abi.params_reference()
     prev = to_dev(mg.initial_prev(), torch)
-    for f, (cam, old, tm) in enumerate(mg.sequence_inputs()):
+    for f, (cam, old, tm) in enumerate(mg.golden_sequence(golden)):
         cur = torch.zeros((mg.SEQ_H, mg.SEQ_W, 4), dtype=torch.float32, device="cuda")
         mask = torch.full((mg.SEQ_H, mg.SEQ_W), float("nan"), dtype=torch.float32, device="cuda")
         ctx.render(cam, old, tm, params, prev, cur, mask, 0)
@@ -111,9 +111,7 @@ def test_reference_sequence_against_golden(ref_ctx, golden):
 
 def test_dispatch_quirk_against_golden(ref_ctx, golden):
     ctx, vol = ref_ctx
-    cam = scenes.look((0.0, 0.0, 2.0), 0.0, mg.SEQ_PITCH, 45.0, mg.QUIRK_W, mg.QUIRK_H)
-    tm = abi.time_init()
-    tm.frame_count_mod16 = mg.QUIRK_FRAME
+    cam, tm = mg.ubos_from(golden["quirk_ubo"], abi.CameraUBO, abi.TimeUBO)
     prev = np.random.default_rng(3).random((mg.QUIRK_H, mg.QUIRK_W, 4), dtype=np.float32)
     g, gm, _ = gpu_render(ctx, cam, cam, tm, abi.params_reference(), prev, mg.QUIRK_W, mg.QUIRK_H, 0)
     assert_hdr_close(g, golden["quirk_rgba"], "quirk")
@@ -122,7 +120,8 @@ def test_dispatch_quirk_against_golden(ref_ctx, golden):
 
 
 def test_txaa_bit_exact(ctx, oracle, golden):
-    cam, old, tm, cur, hist = mg.txaa_inputs()
+    _, _, _, cur, hist = mg.txaa_inputs()
+    cam, old, tm = mg.ubos_from(golden["txaa_ubo"], abi.CameraUBO, abi.CameraUBO, abi.TimeUBO)
     for params in (abi.params_reference(), abi.params_config()):
         want = oracle.txaa(cam, old, tm, params, cur, hist)
         out = torch.zeros_like(to_dev(cur, torch))
