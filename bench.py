@@ -211,7 +211,7 @@ def run_gb300(args) -> int:
     ctx.set_timing(True)
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    kern = {"reproject_ms": [], "march_ms": [], "txaa_ms": []}
+    kern = {"reproject_ms": [], "march_ms": [], "resolve_ms": []}
     clocks = ClockSampler(local)
     if world > 1:
         dist.barrier()

@@ -149,8 +149,17 @@ typedef struct mt_kernel_times {
     float reproject_ms;
     float march_ms;
     float txaa_ms;
-    int32_t _pad;
+    float resolve_ms; /* reprojection fused with TXAA (mt_render_frame) */
 } mt_kernel_times;
+
+/* Launch-shape choices of the kernels.  Results do not depend on them (the
+ * tests hold every choice to the same output); only speed does. */
+typedef struct mt_tuning {
+    int32_t march_lanes;  /* lanes that march one ray together: 1, 4, 8 or 16; 0 = chosen from the ray count */
+    int32_t fused_resolve; /* mt_render_frame: 0 = reprojection, march, TXAA as three launches (default);
+                            * 1 = march, then reprojection fused with TXAA */
+    int32_t _reserved[6];
+} mt_tuning;
 
 /* One view of a batched render (config 3). */
 typedef struct mt_view {
@@ -234,6 +243,18 @@ MT_API mt_status mt_render(mt_ctx* ctx, const mt_camera_ubo* camera, const mt_ca
                            float* cur_rgba, float* godray_mask, int width, int height, uint32_t flags,
                            void* stream);
 
+/* One whole frame: the reprojection and raymarch of mt_render and the TXAA
+ * resolve of mt_txaa (with mt_tuning.fused_resolve, the raymarch then the
+ * reprojection fused with TXAA in a second launch).  cur_rgba receives the
+ * raw frame (what the next frame reprojects from, as with mt_render), out_rgba
+ * the resolved frame (the next frame's TXAA history).  Results equal
+ * mt_render followed by mt_txaa(current = cur_rgba, history_rgba, out_rgba).
+ * With MT_RENDER_FULL every pixel is marched and prev_rgba is not read. */
+MT_API mt_status mt_render_frame(mt_ctx* ctx, const mt_camera_ubo* camera, const mt_camera_ubo* camera_old,
+                                 const mt_time_ubo* time, const mt_params* params, const float* prev_rgba,
+                                 float* cur_rgba, const float* history_rgba, float* out_rgba,
+                                 float* godray_mask, int width, int height, uint32_t flags, void* stream);
+
 /* TXAA resolve (postProcess_TXAA.frag:223-269) of `current` against
  * `history` (the previous resolved frame), written to `out` (distinct from
  * both).  Device pointers; stream-ordered. */
@@ -248,6 +269,17 @@ MT_API mt_status mt_render_batch(mt_ctx* ctx, const mt_view* views, int n_views,
 /* Counters accumulated by render calls made with MT_RENDER_COUNT since the
  * last reset.  Synchronises the stream. */
 MT_API mt_status mt_get_stats(mt_ctx* ctx, mt_stats* out, int reset, void* stream);
+
+/* Launch-shape tuning (no counterpart in the reference, whose workgroup is a
+ * fixed 32x32, cloudRayMarch.comp:4-5). */
+MT_API mt_status mt_set_tuning(mt_ctx* ctx, const mt_tuning* tuning);
+MT_API mt_status mt_get_tuning(mt_ctx* ctx, mt_tuning* tuning);
+
+/* Numerical self-test of the kernels' division by a reused denominator:
+ * out_rdiv[i] is that routine's a[i] / b[i], out_ieee[i] the device's IEEE
+ * division.  The two must agree bit for bit.  Device pointers. */
+MT_API mt_status mt_selftest_division(mt_ctx* ctx, const float* a, const float* b, float* out_rdiv,
+                                      float* out_ieee, int n, void* stream);
 
 /* Per-kernel CUDA-event timing (no counterpart in the reference, which only
  * reports frame rates read off externally, README.md:266-294).  While on,

@@ -105,9 +105,13 @@ class Stats(C.Structure):
     ]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("march_lanes", C.c_int32), ("fused_resolve", C.c_int32), ("_reserved", C.c_int32 * 6)]
+
+
 class KernelTimes(C.Structure):
     _fields_ = [("reproject_ms", C.c_float), ("march_ms", C.c_float), ("txaa_ms", C.c_float),
-                ("_pad", C.c_int32)]
+                ("resolve_ms", C.c_float)]
 
 
 class View(C.Structure):
@@ -152,10 +156,15 @@ SIGNATURES = {
     "mt_download_volumes_16": (C.c_int, [_P, C.c_int, _P, _P, _P, _P, C.c_int]),
     "mt_render": (C.c_int, [_P, C.POINTER(CameraUBO), C.POINTER(CameraUBO), C.POINTER(TimeUBO),
                             C.POINTER(Params), _P, _P, _P, C.c_int, C.c_int, C.c_uint32, _P]),
+    "mt_render_frame": (C.c_int, [_P, C.POINTER(CameraUBO), C.POINTER(CameraUBO), C.POINTER(TimeUBO),
+                                  C.POINTER(Params), _P, _P, _P, _P, _P, C.c_int, C.c_int, C.c_uint32, _P]),
     "mt_txaa": (C.c_int, [_P, C.POINTER(CameraUBO), C.POINTER(CameraUBO), C.POINTER(TimeUBO),
                           C.POINTER(Params), _P, _P, _P, C.c_int, C.c_int, _P]),
     "mt_render_batch": (C.c_int, [_P, C.POINTER(View), C.c_int, _P]),
     "mt_get_stats": (C.c_int, [_P, C.POINTER(Stats), C.c_int, _P]),
+    "mt_set_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
+    "mt_get_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
+    "mt_selftest_division": (C.c_int, [_P, _P, _P, _P, _P, C.c_int, _P]),
     "mt_set_timing": (C.c_int, [_P, C.c_int]),
     "mt_get_kernel_times": (C.c_int, [_P, C.POINTER(KernelTimes)]),
 }

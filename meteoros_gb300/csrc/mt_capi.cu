@@ -33,8 +33,10 @@ struct mt_ctx {
     bool have_base = false, have_detail = false, have_curl = false;
     unsigned long long* stats = nullptr;      // 4 counters
     bool timing = false;
-    cudaEvent_t ev[6] = {};                   // reproject, march, txaa (start, end)
-    bool ran[3] = {false, false, false};
+    cudaEvent_t ev[8] = {};                   // reproject, march, txaa, resolve (start, end)
+    bool ran[4] = {false, false, false, false};
+    int march_lanes = 0;                      // step-parallel lanes per ray (mt_set_tuning); 0 = auto
+    int fused_resolve = 0;                    // mt_render_frame: reprojection fused with TXAA
 };
 
 namespace {
@@ -174,6 +176,13 @@ mt_status build_march_args(mt_ctx* ctx, const mt_camera_ubo* cam, const mt_camer
     a->groups_x = mt::march_groups(w);
     a->groups_y = mt::march_groups(h);
     a->flags = flags;
+    a->lanes = ctx->march_lanes;
+    if (a->lanes == 0) {
+        // Auto: enough rays fill the GPU one lane per ray; fewer rays (a
+        // checkerboard frame marches 1/16 of the pixels) get 4 lanes each.
+        const long long rays = full ? (long long)w * h : (long long)a->groups_x * a->groups_y;
+        a->lanes = rays >= 262144 ? 1 : 4;
+    }
     return MT_OK;
 }
 
@@ -353,11 +362,41 @@ MT_API mt_status mt_render(mt_ctx* ctx, const mt_camera_ubo* camera, const mt_ca
                                     height, flags, &a);
     if (st != MT_OK) return st;
     if ((st = bind_device(ctx)) != MT_OK) return st;
-    mt::LaunchEvents ev{{ctx->ev[0], ctx->ev[1]}, {ctx->ev[2], ctx->ev[3]}, ctx->timing};
+    mt::LaunchEvents ev{{ctx->ev[0], ctx->ev[1]}, {ctx->ev[2], ctx->ev[3]}, {ctx->ev[6], ctx->ev[7]}, ctx->timing};
     MT_CUDA(ctx, mt::launch_render(a, (cudaStream_t)stream, &ev));
     if (ctx->timing) {
         ctx->ran[0] = !(flags & MT_RENDER_FULL) || ctx->ran[0];
         ctx->ran[1] = true;
+    }
+    return MT_OK;
+}
+
+MT_API mt_status mt_render_frame(mt_ctx* ctx, const mt_camera_ubo* camera, const mt_camera_ubo* camera_old,
+                                 const mt_time_ubo* time, const mt_params* params, const float* prev_rgba,
+                                 float* cur_rgba, const float* history_rgba, float* out_rgba, float* godray_mask,
+                                 int width, int height, uint32_t flags, void* stream) {
+    if (!ctx) return MT_ERR_INVALID_ARG;
+    mt::MarchArgs a;
+    mt_status st = build_march_args(ctx, camera, camera_old, time, params, prev_rgba, cur_rgba, godray_mask, width,
+                                    height, flags, &a);
+    if (st != MT_OK) return st;
+    if (!history_rgba || !out_rgba) return fail(ctx, MT_ERR_INVALID_ARG, "history and out must not be NULL");
+    if (!aligned(history_rgba, 16) || !aligned(out_rgba, 16))
+        return fail(ctx, MT_ERR_INVALID_ARG, "images must be 16-byte aligned");
+    if (out_rgba == cur_rgba || out_rgba == history_rgba || out_rgba == prev_rgba)
+        return fail(ctx, MT_ERR_INVALID_ARG, "out_rgba must differ from cur, prev and history");
+    if (history_rgba == cur_rgba)
+        return fail(ctx, MT_ERR_INVALID_ARG, "history_rgba must differ from cur_rgba");
+    a.history = (const float4*)history_rgba;
+    a.out = (float4*)out_rgba;
+    a.fused_resolve = ctx->fused_resolve;
+    if ((st = bind_device(ctx)) != MT_OK) return st;
+    mt::LaunchEvents ev{{ctx->ev[0], ctx->ev[1]}, {ctx->ev[2], ctx->ev[3]}, {ctx->ev[6], ctx->ev[7]}, ctx->timing};
+    MT_CUDA(ctx, mt::launch_frame(a, (cudaStream_t)stream, &ev));
+    if (ctx->timing) {
+        ctx->ran[0] = ctx->ran[0] || (!(flags & MT_RENDER_FULL) && !ctx->fused_resolve);
+        ctx->ran[1] = true;
+        ctx->ran[3] = true;
     }
     return MT_OK;
 }
@@ -421,6 +460,40 @@ MT_API mt_status mt_get_stats(mt_ctx* ctx, mt_stats* out, int reset, void* strea
     return MT_OK;
 }
 
+MT_API mt_status mt_set_tuning(mt_ctx* ctx, const mt_tuning* t) {
+    if (!ctx) return MT_ERR_INVALID_ARG;
+    if (!t) return fail(ctx, MT_ERR_INVALID_ARG, "tuning must not be NULL");
+    if (t->march_lanes != 0 && t->march_lanes != 1 && t->march_lanes != 4 && t->march_lanes != 8 &&
+        t->march_lanes != 16)
+        return fail(ctx, MT_ERR_INVALID_ARG, "march_lanes must be 0 (auto), 1, 4, 8 or 16 (got %d)",
+                    t->march_lanes);
+    if (t->fused_resolve != 0 && t->fused_resolve != 1)
+        return fail(ctx, MT_ERR_INVALID_ARG, "fused_resolve must be 0 or 1");
+    ctx->march_lanes = t->march_lanes;
+    ctx->fused_resolve = t->fused_resolve;
+    return MT_OK;
+}
+
+MT_API mt_status mt_get_tuning(mt_ctx* ctx, mt_tuning* t) {
+    if (!ctx) return MT_ERR_INVALID_ARG;
+    if (!t) return fail(ctx, MT_ERR_INVALID_ARG, "tuning must not be NULL");
+    std::memset(t, 0, sizeof(*t));
+    t->march_lanes = ctx->march_lanes;
+    t->fused_resolve = ctx->fused_resolve;
+    return MT_OK;
+}
+
+MT_API mt_status mt_selftest_division(mt_ctx* ctx, const float* a, const float* b, float* out_rdiv, float* out_ieee,
+                                      int n, void* stream) {
+    if (!ctx) return MT_ERR_INVALID_ARG;
+    if (n < 0 || (n > 0 && (!a || !b || !out_rdiv || !out_ieee)))
+        return fail(ctx, MT_ERR_INVALID_ARG, "bad self-test buffers");
+    mt_status st;
+    if ((st = bind_device(ctx)) != MT_OK) return st;
+    MT_CUDA(ctx, mt::launch_selftest_division(a, b, out_rdiv, out_ieee, n, (cudaStream_t)stream));
+    return MT_OK;
+}
+
 MT_API mt_status mt_set_timing(mt_ctx* ctx, int enabled) {
     if (!ctx) return MT_ERR_INVALID_ARG;
     mt_status st;
@@ -428,7 +501,7 @@ MT_API mt_status mt_set_timing(mt_ctx* ctx, int enabled) {
     if (enabled && !ctx->ev[0])
         for (cudaEvent_t& e : ctx->ev) MT_CUDA(ctx, cudaEventCreate(&e));
     ctx->timing = enabled != 0;
-    ctx->ran[0] = ctx->ran[1] = ctx->ran[2] = false;
+    ctx->ran[0] = ctx->ran[1] = ctx->ran[2] = ctx->ran[3] = false;
     return MT_OK;
 }
 
@@ -439,8 +512,8 @@ MT_API mt_status mt_get_kernel_times(mt_ctx* ctx, mt_kernel_times* out) {
     if (!ctx->ev[0]) return MT_OK;
     mt_status st;
     if ((st = bind_device(ctx)) != MT_OK) return st;
-    float* dst[3] = {&out->reproject_ms, &out->march_ms, &out->txaa_ms};
-    for (int k = 0; k < 3; ++k) {
+    float* dst[4] = {&out->reproject_ms, &out->march_ms, &out->txaa_ms, &out->resolve_ms};
+    for (int k = 0; k < 4; ++k) {
         if (!ctx->ran[k]) continue;
         MT_CUDA(ctx, cudaEventSynchronize(ctx->ev[2 * k + 1]));
         MT_CUDA(ctx, cudaEventElapsedTime(dst[k], ctx->ev[2 * k], ctx->ev[2 * k + 1]));

@@ -58,9 +58,40 @@ MT_HD float gsmoothstep(float e0, float e1, float x) {
 // cvt.rzi.s32.f32: truncation, saturating to the int range, NaN -> 0.
 MT_HD int f2i(float v) { return __float2int_rz(v); }
 
+// ---------------------------------------------------------------------------
+// Division by a reused denominator, bit-identical to IEEE a / b.
+// With y = RN(1/b) and q0 = RN(a*y) (within one ulp of a/b), the residual
+// r = a - q0*b is exact in one FMA and q = RN(q0 + r*y) is the correctly
+// rounded quotient (Markstein, "Computation of elementary functions on the
+// IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1), 1990).  The
+// theorem excludes overflow and underflow, so zero, tiny, huge and non-finite
+// quotients (and the sign of a zero quotient) go through the IEEE division.
+// ---------------------------------------------------------------------------
+struct Rcp {
+    float b, y;
+};
+// The IEEE division, out of line: one shared copy keeps the callers small in
+// the instruction cache (the march loop is instruction-fetch bound otherwise).
+__device__ __noinline__ float div_ieee(float a, float b) { return a / b; }
+MT_HD Rcp make_rcp(float b) { return Rcp{b, div_ieee(1.0f, b)}; }
+MT_HD float rdiv(float a, Rcp r) {
+    const float q0 = __fmul_rn(a, r.y);
+    const float e = __fmaf_rn(-q0, r.b, a);
+    const float q = __fmaf_rn(e, r.y, q0);
+    const float aq = fabsf(q);
+    if (aq >= 0x1p-100f && aq <= 0x1p100f) return q;
+    return div_ieee(a, r.b);
+}
+__device__ __noinline__ float pow_nl(float x, float y) { return powf(x, y); }
+
 MT_HD float dot3(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 MT_HD float length3(f3 a) { return sqrtf(dot3(a, a)); }
 MT_HD f3 normalize3(f3 a) { return a / length3(a); }
+// normalize(v) = v / length(v), the three divisions sharing one reciprocal.
+MT_HD f3 normalize3_r(f3 a) {
+    const Rcp r = make_rcp(length3(a));
+    return f3{rdiv(a.x, r), rdiv(a.y, r), rdiv(a.z, r)};
+}
 MT_HD f3 cross3(f3 a, f3 b) { return f3{a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y}; }
 MT_HD f3 mix3(f3 x, f3 y, float a) { return f3{gmix(x.x, y.x, a), gmix(x.y, y.y, a), gmix(x.z, y.z, a)}; }
 MT_HD f4v min4(f4v a, f4v b) { return f4v{gmin(a.x, b.x), gmin(a.y, b.y), gmin(a.z, b.z), gmin(a.w, b.w)}; }
@@ -79,8 +110,23 @@ MT_HD f4v lerp4(f4v p, f4v q, float t) {
     return f4v{lerp1(p.x, q.x, t), lerp1(p.y, q.y, t), lerp1(p.z, q.z, t), lerp1(p.w, q.w, t)};
 }
 
-MT_HD f4v unpack_rgba8(uint32_t v) {
-    return f4v{(float)(v & 0xffu), (float)((v >> 8) & 0xffu), (float)((v >> 16) & 0xffu), (float)(v >> 24)};
+// A texel byte as a float without a conversion instruction: byte_perm builds
+// the word 0x4B0000bb, which is the float 2^23 + bb exactly (the byte lands in
+// the low mantissa bits).  Interpolation works on these biased values:
+// p = P - 2^23 and q - p = Q - P are exact, so lerp(p, q, t) = p + t*(q - p)
+// is reproduced bit for bit.
+MT_HD float biased_byte(uint32_t word, unsigned c) { return __int_as_float(__byte_perm(word, 0x4B000000u, 0x7540u | c)); }
+constexpr float kByteBias = 8388608.0f;
+
+MT_HD f4v lerp_texels(uint32_t w0, uint32_t w1, float t) {
+    f4v r;
+    float* o = &r.x;
+#pragma unroll
+    for (unsigned c = 0; c < 4; ++c) {
+        const float P = biased_byte(w0, c), Q = biased_byte(w1, c);
+        o[c] = (P - kByteBias) + t * (Q - P);
+    }
+    return r;
 }
 
 // ---------------------------------------------------------------------------
@@ -104,10 +150,10 @@ template <int N> MT_HD f4v tex3_u8(const uint32_t* __restrict__ vol, f3 s) {
     uint32_t t010 = __ldg(p0 + y1 * N + x0), t110 = __ldg(p0 + y1 * N + x1);
     uint32_t t001 = __ldg(p1 + y0 * N + x0), t101 = __ldg(p1 + y0 * N + x1);
     uint32_t t011 = __ldg(p1 + y1 * N + x0), t111 = __ldg(p1 + y1 * N + x1);
-    f4v c00 = lerp4(unpack_rgba8(t000), unpack_rgba8(t100), a);
-    f4v c10 = lerp4(unpack_rgba8(t010), unpack_rgba8(t110), a);
-    f4v c01 = lerp4(unpack_rgba8(t001), unpack_rgba8(t101), a);
-    f4v c11 = lerp4(unpack_rgba8(t011), unpack_rgba8(t111), a);
+    f4v c00 = lerp_texels(t000, t100, a);
+    f4v c10 = lerp_texels(t010, t110, a);
+    f4v c01 = lerp_texels(t001, t101, a);
+    f4v c11 = lerp_texels(t011, t111, a);
     f4v c0 = lerp4(c00, c10, b);
     f4v c1 = lerp4(c01, c11, b);
     return lerp4(c0, c1, g) * (1.0f / 255.0f);
@@ -121,8 +167,8 @@ template <int N> MT_HD f4v tex2_u8(const uint32_t* __restrict__ img, float sx, f
     float a = u - fu, b = v - fv;
     unsigned iu = (unsigned)f2i(fu), iv = (unsigned)f2i(fv);
     unsigned x0 = iu & M, x1 = (iu + 1u) & M, y0 = iv & M, y1 = (iv + 1u) & M;
-    f4v c0 = lerp4(unpack_rgba8(__ldg(img + y0 * N + x0)), unpack_rgba8(__ldg(img + y0 * N + x1)), a);
-    f4v c1 = lerp4(unpack_rgba8(__ldg(img + y1 * N + x0)), unpack_rgba8(__ldg(img + y1 * N + x1)), a);
+    f4v c0 = lerp_texels(__ldg(img + y0 * N + x0), __ldg(img + y0 * N + x1), a);
+    f4v c1 = lerp_texels(__ldg(img + y1 * N + x0), __ldg(img + y1 * N + x1), a);
     return lerp4(c0, c1, b) * (1.0f / 255.0f);
 }
 

@@ -26,6 +26,10 @@ struct MarchArgs {
     int32_t width, height;
     int32_t groups_x, groups_y;  // 4x4 blocks covered by the reference's raymarch dispatch
     uint32_t flags;
+    int32_t lanes;               // lanes marching one ray together: 1, 4, 8 or 16
+    const float4* history;       // mt_render_frame only: previous resolved frame
+    float4* out;                 // mt_render_frame only: resolved frame
+    int32_t fused_resolve;       // mt_render_frame: 1 = reprojection fused with TXAA
 };
 
 struct TxaaArgs {
@@ -50,11 +54,16 @@ struct NoiseOut {
 struct LaunchEvents {
     cudaEvent_t reproject[2];
     cudaEvent_t march[2];
+    cudaEvent_t resolve[2];
     bool on;
 };
 
 cudaError_t launch_render(const MarchArgs& a, cudaStream_t s, const LaunchEvents* ev);
 cudaError_t launch_txaa(const TxaaArgs& a, cudaStream_t s, const cudaEvent_t* ev);
+// The raymarch, then reprojection fused with TXAA (a.history -> a.out).
+cudaError_t launch_frame(const MarchArgs& a, cudaStream_t s, const LaunchEvents* ev);
+cudaError_t launch_selftest_division(const float* a, const float* b, float* out_rdiv, float* out_ieee, int n,
+                                     cudaStream_t s);
 cudaError_t launch_generate_base(uint32_t seed, NoiseOut o, cudaStream_t s);
 cudaError_t launch_generate_detail(uint32_t seed, NoiseOut o, cudaStream_t s);
 cudaError_t launch_generate_curl(uint32_t seed, NoiseOut o, cudaStream_t s);

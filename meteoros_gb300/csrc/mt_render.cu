@@ -23,6 +23,7 @@ namespace mt {
 
 struct Frame {
     float R, Rin, Rout, thickness, inner_alt;
+    Rcp r_thick, r_period, r_weather;  // per-frame denominators (see rdiv)
 };
 
 MT_HD Frame make_frame(const mt_params& p) {
@@ -32,8 +33,19 @@ MT_HD Frame make_frame(const mt_params& p) {
     F.Rout = p.shell_outer_radius;
     F.thickness = F.Rout - F.Rin;
     F.inner_alt = F.Rin - F.R;
+    F.r_thick = make_rcp(F.thickness);
+    F.r_period = make_rcp(p.noise_period);
+    F.r_weather = make_rcp(p.weather_scale);
     return F;
 }
+
+// remap() whose range width omax - omin is known ahead: the quotient through
+// the correctly rounded reciprocal of that width (rdiv).
+MT_HD float remap_r(float v, float omin, Rcp width, float nmin, float nmax) {
+    return nmin + ((rdiv(v - omin, width)) * (nmax - nmin));
+}
+// The reciprocal of a compile-time width, rounded once by the compiler.
+#define MT_RCP(omin, omax) (Rcp{(omax) - (omin), 1.0f / ((omax) - (omin))})
 
 struct Ray {
     f3 origin, direction;
@@ -163,22 +175,25 @@ MT_HD float remap_clamped_ba(float v, float omin, float omax, float nmin, float 
 MT_HD float relative_height(const Frame& F, f3 point, f3 ec, f3 startPos, f3 rayDir, f3 eye) {
     float lenCam = length3(point - eye);
     float lenInner = length3(startPos - eye);
-    f3 p2e = normalize3(point - ec);
+    f3 p2e = normalize3_r(point - ec);
     float cosTheta = dot3(rayDir, p2e);
     float num = fabsf(cosTheta * (lenCam - lenInner));
-    return num / F.thickness;
+    return rdiv(num, F.r_thick);
 }
 
 // cloudRayMarch.comp:188-191
 MT_HD f3 relative_position(const Frame& F, f3 pos, f3 ec) {
-    return (pos - f3{ec.x, F.inner_alt, ec.z}) / F.thickness;
+    const f3 d = pos - f3{ec.x, F.inner_alt, ec.z};
+    return f3{rdiv(d.x, F.r_thick), rdiv(d.y, F.r_thick), rdiv(d.z, F.r_thick)};
 }
 
 // cloudRayMarch.comp:475-487
 MT_HD float height_gradient(float h, float type) {
     h = gclamp(h, 0.0f, 1.0f);
-    float stratocumulus = gmax(0.0f, remap(h, 0.0f, 0.25f, 0.0f, 1.0f) * remap(h, 0.3f, 0.65f, 1.0f, 0.0f));
-    float stratus = gmax(0.0f, remap(h, 0.0f, 0.1f, 0.0f, 1.0f) * remap(h, 0.2f, 0.3f, 1.0f, 0.0f));
+    float stratocumulus = gmax(0.0f, remap_r(h, 0.0f, MT_RCP(0.0f, 0.25f), 0.0f, 1.0f) *
+                                         remap_r(h, 0.3f, MT_RCP(0.3f, 0.65f), 1.0f, 0.0f));
+    float stratus = gmax(0.0f, remap_r(h, 0.0f, MT_RCP(0.0f, 0.1f), 0.0f, 1.0f) *
+                                   remap_r(h, 0.2f, MT_RCP(0.2f, 0.3f), 1.0f, 0.0f));
     float a = gmix(stratus, stratocumulus, gclamp(type * 2.0f, 0.0f, 1.0f));
     float b = gmix(stratocumulus, stratus, gclamp((type - 0.5f) * 2.0f, 0.0f, 1.0f));
     return gmix(a, b, type);
@@ -186,6 +201,8 @@ MT_HD float height_gradient(float h, float type) {
 
 struct Weather {
     float lo, mul, type;
+    float hgrad;  // height gradient at the primary sample, shared by its light samples
+    Rcp r_lo;     // 1 - lo, the coverage remap's width, shared by the step's samples
 };
 
 struct Tex {
@@ -195,19 +212,20 @@ struct Tex {
     const uint32_t* weather;
 };
 
-MT_HD Weather weather_at(const mt_params& p, const Tex& tx, f3 pos, f3 ec) {
+MT_HD Weather weather_at(const mt_params& p, const Frame& F, const Tex& tx, f3 pos, f3 ec) {
     Weather w;
+    w.hgrad = 1.0f;
     if (p.coverage_mode == 0) {
         w.lo = p.coverage;
         w.mul = p.coverage;
         w.type = 0.0f;
-        return w;
+    } else {
+        f4v wd = tex2_u8<MT_WEATHER_N>(tx.weather, rdiv(pos.x - ec.x, F.r_weather), rdiv(pos.z - ec.z, F.r_weather));
+        w.lo = 1.0f - wd.x;
+        w.mul = wd.x;
+        w.type = wd.z;
     }
-    const float ws = p.weather_scale;
-    f4v wd = tex2_u8<MT_WEATHER_N>(tx.weather, (pos.x - ec.x) / ws, (pos.z - ec.z) / ws);
-    w.lo = 1.0f - wd.x;
-    w.mul = wd.x;
-    w.type = wd.z;
+    w.r_lo = make_rcp(1.0f - w.lo);
     return w;
 }
 
@@ -217,8 +235,14 @@ MT_HD float sample_low_frequency(const mt_params& p, const Tex& tx, f3 point, fl
     float fbm = (n.y * 0.625f) + (n.z * 0.25f) + (n.w * 0.125f);
     fbm = gclamp(fbm, 0.0f, 1.0f);
     float baseCloud = remap_clamped(n.x, (fbm - 0.9f), 1.0f, 0.0f, 1.0f);
-    if (p.height_gradient) baseCloud = baseCloud * height_gradient(relH, wt.type);
-    float bc = remap_clamped_ba(baseCloud, wt.lo, 1.0f, 0.0f, 1.0f);
+    // getDensityHeightGradientForPoint(relH, type): every call of a step passes
+    // the primary sample's height and weather, so it is evaluated once per step
+    // (Weather::hgrad).
+    if (p.height_gradient) baseCloud = baseCloud * wt.hgrad;
+    // remapClampedBeforeAndAfter(baseCloud, lo, 1, 0, 1) with its width 1 - lo
+    // shared by the step's samples
+    float v = gclamp(baseCloud, wt.lo, 1.0f);
+    float bc = gclamp(0.0f + ((rdiv(v - wt.lo, wt.r_lo)) * (1.0f - 0.0f)), 0.0f, 1.0f);
     return bc * wt.mul;
 }
 
@@ -233,7 +257,17 @@ MT_HD float erosion_modifier(const Tex& tx, f3 point, float h) {
     float hfbm = (hf.x * 0.625f) + (hf.y * 0.25f) + (hf.z * 0.125f);
     return gclamp(gmix(hfbm, 1.0f - hfbm, gclamp(h * 2.0f, 0.0f, 1.0f)), 0.0f, 1.0f);
 }
-MT_HD float erode(float baseCloud, float modifier) { return remap(baseCloud, modifier * 0.005f, 1.0f, 0.0f, 1.0f); }
+struct Erosion {
+    float lo;  // high_freq_modifier * 0.005
+    Rcp r;     // 1 - lo, shared by the step's seven erosions
+};
+MT_HD Erosion make_erosion(float modifier) {
+    Erosion e;
+    e.lo = modifier * 0.005f;
+    e.r = make_rcp(1.0f - e.lo);
+    return e;
+}
+MT_HD float erode(float baseCloud, const Erosion& e) { return remap_r(baseCloud, e.lo, e.r, 0.0f, 1.0f); }
 
 // cloudRayMarch.comp:295-306
 MT_HD float henyey_greenstein(float c, float e) {
@@ -242,19 +276,21 @@ MT_HD float henyey_greenstein(float c, float e) {
     return (num / den) * 0.07957747154594767f;
 }
 
-// cloudRayMarch.comp:331-388
-MT_HD float light_energy(float h, float dl, float ds, float phase, float cos_angle, float brightness) {
-    float primary = expf(-dl);
-    float secondary = expf(-dl);
-    float att = gmax(remap(cos_angle, 0.7f, 1.0f, secondary, secondary * 0.25f), primary);
-    float depth = 0.05f + powf(ds, gclamp(remap(h * 0.125f, 0.3f, 0.85f, 0.5f, 2.0f), 0.5f, 2.0f));
-    float vert = powf(gclamp(remap(h * 1.5f, 0.07f, 0.34f, 0.1f, 1.0f), 0.1f, 1.0f), 0.8f);
+// cloudRayMarch.comp:331-388.  cos_q = (cos_angle - 0.7) / (1.0 - 0.7), the
+// ray-constant quotient of the attenuation remap (:341-343).
+MT_HD float light_energy(float h, float dl, float ds, float phase, float cos_q, float brightness) {
+    const float primary = expf(-dl);
+    const float secondary = primary;  // exp(-dl) twice in the reference (:334, :340)
+    float att = gmax(secondary + (cos_q * (secondary * 0.25f - secondary)), primary);
+    float depth = 0.05f + pow_nl(ds, gclamp(remap_r(h * 0.125f, 0.3f, MT_RCP(0.3f, 0.85f), 0.5f, 2.0f), 0.5f, 2.0f));
+    float vert = pow_nl(gclamp(remap_r(h * 1.5f, 0.07f, MT_RCP(0.07f, 0.34f), 0.1f, 1.0f), 0.1f, 1.0f), 0.8f);
     float in_scatter = depth * vert;
     return att * primary * in_scatter * phase * brightness;
 }
 
-// cloudRayMarch.comp:401-467 (Preetham)
-MT_HD f3 atmosphere_color(const mt_params& p, f3 dir, f3 sunDir, float sunIntensity) {
+// cloudRayMarch.comp:401-467 (Preetham).  Once per ray: kept out of line so
+// the march loop stays small in the instruction cache.
+__device__ __noinline__ f3 atmosphere_color(const mt_params& p, f3 dir, f3 sunDir, float sunIntensity) {
     const f3 skySun = ld3(p.sky_sun_pos);
     const float PI = 3.14159265f;
     sunDir = normalize3(sunDir);
@@ -298,24 +334,27 @@ struct Counts {
     unsigned primary, light, rays;
 };
 
-// cloudRayMarch.comp:565-688
-MT_HD f3 ray_march(const mt_params& p, const Frame& F, const Tex& tx, const mt_time_ubo& tm, const Ray& ray, f3 ec,
-                   f3 startPos, float start_t, float end_t, int pixelID, float& accum, Counts& cnt) {
-    float _dot = dot3(ray.direction, f3{0.0f, 1.0f, 0.0f});
-    float maxSteps;
-    if (p.steps_min == p.steps_max)
-        maxSteps = (float)p.steps_min;
-    else
-        maxSteps = floorf(gmix((float)p.steps_min, (float)p.steps_max, 1.0f - _dot));
-    const float thick = end_t - start_t;
-    const float stepSize = thick / maxSteps;
-    float transmittance = 1.0f;
-    f3 color{0.0f, 0.0f, 0.0f};
+// Per-ray constants of cloudRayMarch.comp:565-624, shared by every step.
+struct RayConsts {
+    Ray ray;
+    f3 ec, startPos;
+    f3 kernel[6];
+    f3 wind, skew;
+    float stepSize, cos_angle, cos_q, HG_light, total_time;
+    int pixelID;
+};
 
+__device__ __noinline__ void ray_consts(const mt_params& p, const mt_time_ubo& tm, const Ray& ray, f3 ec,
+                                        f3 startPos, float stepSize, int pixelID, RayConsts& rc) {
+    rc.ray = ray;
+    rc.ec = ec;
+    rc.startPos = startPos;
+    rc.stepSize = stepSize;
+    rc.pixelID = pixelID;
     const f3 lightDir = normalize3(ld3(p.sun_light_pos) - ray.origin);
-    const float cos_angle = dot3(normalize3(ray.direction), lightDir);
-    const float HG_light = gmax(henyey_greenstein(cos_angle, 0.6f), 0.7f * henyey_greenstein(cos_angle, 0.99f - 0.1f));
-
+    rc.cos_angle = dot3(normalize3(ray.direction), lightDir);
+    rc.cos_q = (rc.cos_angle - 0.7f) / (1.0f - 0.7f);
+    rc.HG_light = gmax(henyey_greenstein(rc.cos_angle, 0.6f), 0.7f * henyey_greenstein(rc.cos_angle, 0.99f - 0.1f));
     float ax = fabsf(lightDir.x), ay = fabsf(lightDir.y), az = fabsf(lightDir.z);
     f3 maxComp;
     if (ax > ay && ax > az)
@@ -326,57 +365,124 @@ MT_HD f3 ray_march(const mt_params& p, const Frame& F, const Tex& tx, const mt_t
         maxComp = f3{0.0f, 0.0f, az};
     f3 zC = cross3(lightDir, maxComp);
     f3 xC = cross3(zC, lightDir);
-    f3 kernel[6];
-    kernel[0] = mat3mul(xC, lightDir, zC, f3{0.1f, 0.25f, -0.15f});
-    kernel[1] = mat3mul(xC, lightDir, zC, f3{0.2f, 0.5f, 0.2f});
-    kernel[2] = mat3mul(xC, lightDir, zC, f3{-0.2f, 0.1f, -0.1f});
-    kernel[3] = mat3mul(xC, lightDir, zC, f3{-0.05f, 0.75f, 0.05f});
-    kernel[4] = mat3mul(xC, lightDir, zC, f3{-0.1f, 1.0f, 0.0f});
-    kernel[5] = mat3mul(xC, lightDir, zC, f3{0.0f, 3.0f, 0.0f});
+    rc.kernel[0] = mat3mul(xC, lightDir, zC, f3{0.1f, 0.25f, -0.15f});
+    rc.kernel[1] = mat3mul(xC, lightDir, zC, f3{0.2f, 0.5f, 0.2f});
+    rc.kernel[2] = mat3mul(xC, lightDir, zC, f3{-0.2f, 0.1f, -0.1f});
+    rc.kernel[3] = mat3mul(xC, lightDir, zC, f3{-0.05f, 0.75f, 0.05f});
+    rc.kernel[4] = mat3mul(xC, lightDir, zC, f3{-0.1f, 1.0f, 0.0f});
+    rc.kernel[5] = mat3mul(xC, lightDir, zC, f3{0.0f, 3.0f, 0.0f});
+    rc.wind = ld3(p.wind_dir) * p.wind_speed;
+    rc.skew = ld3(p.skew_dir);
+    rc.total_time = tm.time[1];
+}
 
-    const f3 wind = ld3(p.wind_dir) * p.wind_speed;
-    const f3 skew = ld3(p.skew_dir);
-    const float total_time = tm.time[1];
+struct StepOut {
+    int in_cloud;  // baseDensity > 0 (cloudRayMarch.comp:642)
+    float hfd;     // eroded density (:645)
+    float E;       // light energy (:673)
+};
+
+// One iteration of the march loop body (cloudRayMarch.comp:629-678) at
+// parameter t, up to the accumulation: everything that does not depend on the
+// running accumDensity / transmittance.
+MT_HD StepOut eval_step(const mt_params& p, const Frame& F, const Tex& tx, const mt_time_ubo& tm,
+                        const RayConsts& rc, float t) {
+    StepOut o{0, 0.0f, 0.0f};
+    int _index = f2i(gmod((float)(rc.pixelID + f2i(t)), 16.0f));
+    float jx, jy;
+    jitter_offset(tm, _index, 1.0f, 1.0f, false, jx, jy);  // halton values; / 75 below
+    jx = rdiv(jx, MT_RCP(0.0f, 75.0f));
+    jy = rdiv(jy, MT_RCP(0.0f, 75.0f));
+    f3 jd = rc.ray.direction + f3{jx, (jx + jy) * 1.180f, jy};
+    f3 pos = rc.ray.origin + t * jd;
+    f3 sp = relative_position(F, pos, rc.ec);
+    sp = f3{rdiv(sp.x, F.r_period), rdiv(sp.y, F.r_period), rdiv(sp.z, F.r_period)};
+    float relH = relative_height(F, pos, rc.ec, rc.startPos, rc.ray.direction, rc.ray.origin);
+    sp = sp + ((relH * rc.skew) * p.cloud_top_offset) * 0.009f;
+    sp = sp + rc.wind * rc.total_time;
+    Weather wt = weather_at(p, F, tx, pos, rc.ec);
+    if (p.height_gradient) wt.hgrad = height_gradient(relH, wt.type);
+    float baseDensity = sample_low_frequency(p, tx, sp, relH, wt) * 0.380f;
+    if (baseDensity > 0.0f) {
+        const Erosion ero = make_erosion(erosion_modifier(tx, sp, relH));
+        o.in_cloud = 1;
+        o.hfd = erode(baseDensity * 1.4f, ero);
+        float dl = 0.0f;
+        // Kept rolled: six inlined copies of the sampler overflow the
+        // instruction cache (the dominant stall when unrolled).
+#pragma unroll 1
+        for (int i = 0; i < 6; ++i) {
+            f3 lightPos = pos + ((rc.stepSize * rc.kernel[i]) * (float)i);
+            f3 slp = relative_position(F, lightPos, rc.ec);
+            float cbl = sample_low_frequency(p, tx, slp, relH, wt);
+            if (cbl > 0.0f) dl = dl + erode(1.5f * cbl, ero);
+        }
+        o.E = light_energy(relH, dl, baseDensity, rc.HG_light, rc.cos_q, 5.0f);
+    }
+    return o;
+}
+
+// cloudRayMarch.comp:565-688, step-parallel.  A group of G lanes marches one
+// ray: lane j evaluates step c*G + j of chunk c, with t rebuilt by the same
+// serial `t += stepSize` additions as the reference's loop, so every lane sees
+// bit-identical t.  The loop-carried part (accumDensity, transmittance,
+// colour, the early exit) is then applied in step order by an in-group scan;
+// steps past the exit are discarded.  Result, counters and control flow equal
+// the sequential loop's.
+template <int G>
+MT_HD f3 ray_march_group(const mt_params& p, const Frame& F, const Tex& tx, const mt_time_ubo& tm, const Ray& ray,
+                         f3 ec, f3 startPos, float start_t, float end_t, int pixelID, float& accum, Counts& cnt,
+                         unsigned gmask, int lane) {
+    float _dot = dot3(ray.direction, f3{0.0f, 1.0f, 0.0f});
+    float maxSteps;
+    if (p.steps_min == p.steps_max)
+        maxSteps = (float)p.steps_min;
+    else
+        maxSteps = floorf(gmix((float)p.steps_min, (float)p.steps_max, 1.0f - _dot));
+    const float thick = end_t - start_t;
+    const float stepSize = thick / maxSteps;
+    RayConsts rc;
+    ray_consts(p, tm, ray, ec, startPos, stepSize, pixelID, rc);
+    float transmittance = 1.0f;
+    f3 color{0.0f, 0.0f, 0.0f};
     // Iteration guard (not in the reference): a step below the ulp of t would
     // never advance.  A valid ray runs steps or steps+1 iterations.
     const int cap = 2 * f2i(maxSteps) + 8;
-    int it = 0;
-    cnt.rays++;
-    for (float t = start_t; t < end_t; t += stepSize) {
-        if (it++ >= cap) break;
-        cnt.primary++;
-        int _index = f2i(gmod((float)(pixelID + f2i(t)), 16.0f));
-        float jx, jy;
-        jitter_offset(tm, _index, 75.0f, 75.0f, false, jx, jy);
-        f3 jd = ray.direction + f3{jx, (jx + jy) * 1.180f, jy};
-        f3 pos = ray.origin + t * jd;
-        f3 sp = relative_position(F, pos, ec);
-        sp = sp / p.noise_period;
-        float relH = relative_height(F, pos, ec, startPos, ray.direction, ray.origin);
-        sp = sp + ((relH * skew) * p.cloud_top_offset) * 0.009f;
-        sp = sp + wind * total_time;
-        Weather wt = weather_at(p, tx, pos, ec);
-        float baseDensity = sample_low_frequency(p, tx, sp, relH, wt) * 0.380f;
-        if (baseDensity > 0.0f) {
-            float mod = erosion_modifier(tx, sp, relH);
-            float hfd = erode(baseDensity * 1.4f, mod);
-            accum = accum + hfd * 0.5f;
-            float dl = 0.0f;
+    if (lane == 0) cnt.rays++;
+    float t_base = start_t;
+    int s_base = 0;
+    bool done = false;
+    while (!done) {
+        float t = t_base;
+        for (int k = 0; k < lane; ++k) t += stepSize;
+        const int valid = (t < end_t) && (s_base + lane < cap);
+        StepOut o{0, 0.0f, 0.0f};
+        if (valid) o = eval_step(p, F, tx, tm, rc, t);
 #pragma unroll
-            for (int i = 0; i < 6; ++i) {
-                f3 lightPos = pos + ((stepSize * kernel[i]) * (float)i);
-                f3 slp = relative_position(F, lightPos, ec);
-                float cbl = sample_low_frequency(p, tx, slp, relH, wt);
-                if (cbl > 0.0f) dl = dl + erode(1.5f * cbl, mod);
+        for (int k = 0; k < G; ++k) {
+            if (!__shfl_sync(gmask, valid, k, G)) {
+                done = true;
+                break;
             }
-            cnt.light += 6;
-            float E = light_energy(relH, dl, baseDensity, HG_light, cos_angle, 5.0f);
-            transmittance = gmix(transmittance, E, (1.0f - accum));
-            color = color + f3{transmittance, transmittance, transmittance};
+            const int in_cloud = __shfl_sync(gmask, o.in_cloud, k, G);
+            const float hfd = __shfl_sync(gmask, o.hfd, k, G);
+            const float E = __shfl_sync(gmask, o.E, k, G);
+            if (lane == 0) cnt.primary++;
+            if (in_cloud) {
+                accum = accum + hfd * 0.5f;
+                transmittance = gmix(transmittance, E, (1.0f - accum));
+                color = color + f3{transmittance, transmittance, transmittance};
+                if (lane == 0) cnt.light += 6;
+            }
+            if (accum >= p.accum_limit) {
+                accum = 1.0f;
+                done = true;
+                break;
+            }
         }
-        if (accum >= p.accum_limit) {
-            accum = 1.0f;
-            break;
+        if (!done) {
+            t_base = __shfl_sync(gmask, t, G - 1, G) + stepSize;
+            s_base += G;
         }
     }
     return color;
@@ -392,7 +498,11 @@ MT_HD float godray_value(float v, float dir_y) {
     return enc.x * (1.0f / 1.0f) + enc.y * (1.0f / 255.0f) + enc.z * (1.0f / 65025.0f) + enc.w * (1.0f / 16581375.0f);
 }
 
-MT_HD void march_pixel(const MarchArgs& a, const Frame& F, const Tex& tx, int px, int py, Counts& cnt) {
+// cloudRayMarch.comp:690-826 for one pixel, marched by a group of G lanes;
+// lane 0 stores.
+template <int G>
+MT_HD void march_pixel(const MarchArgs& a, const Frame& F, const Tex& tx, int px, int py, Counts& cnt,
+                       unsigned gmask, int lane) {
     const mt_params& p = a.params;
     const int W = a.width, H = a.height;
     const int pixelID = a.time.frame_count_mod16;
@@ -410,15 +520,19 @@ MT_HD void march_pixel(const MarchArgs& a, const Frame& F, const Tex& tx, int px
         f3 cNear = f3{0.0f, 0.16f, 0.51f} * 0.4f;
         f3 c2 = f3{0.0f, 0.73f, 0.95f} * 0.5f;
         bg = mix3(cNear, c2, -ray.direction.y * 5.5f);
-        a.cur[o] = make_float4(bg.x, bg.y, bg.z, 1.0f);
-        if (a.mask) a.mask[o] = 0.0f;
+        if (lane == 0) {
+            a.cur[o] = make_float4(bg.x, bg.y, bg.z, 1.0f);
+            if (a.mask) a.mask[o] = 0.0f;
+        }
         return;
     }
     bg = atmosphere_color(p, ray.direction, ld3(p.sky_sun_pos) - ray.origin, sunIntensity);
     bg = bg * bgMul;
     if (_dot < fade) {
-        a.cur[o] = make_float4(bg.x, bg.y, bg.z, 1.0f);
-        if (a.mask) a.mask[o] = 0.0f;
+        if (lane == 0) {
+            a.cur[o] = make_float4(bg.x, bg.y, bg.z, 1.0f);
+            if (a.mask) a.mask[o] = 0.0f;
+        }
         return;
     }
     f3 ec = eyePos;
@@ -432,7 +546,8 @@ MT_HD void march_pixel(const MarchArgs& a, const Frame& F, const Tex& tx, int px
         out = ray_sphere(ray.origin, ray.direction, ec, F.Rout);
     }
     float accum = 0.0f;
-    f3 res = ray_march(p, F, tx, a.time, ray, ec, in.point, in.t, out.t, pixelID, accum, cnt);
+    f3 res = ray_march_group<G>(p, F, tx, a.time, ray, ec, in.point, in.t, out.t, pixelID, accum, cnt, gmask, lane);
+    if (lane != 0) return;
     float godAccum = accum;
     accum = accum * gsmoothstep(0.0f, 1.0f, gmin(1.0f, remap(ray.direction.y, fade, 0.2f, 0.0f, 1.0f)));
     f3 fc = mix3(bg, res, accum);
@@ -453,13 +568,19 @@ __device__ __forceinline__ void flush_counts(unsigned long long* stats, const Co
     }
 }
 
-// Thread -> marched pixel.  Checkerboard: the reference's group grid covers
-// groups_x x groups_y blocks of 4x4 (Renderer.cpp:713-716); each thread takes
-// one block and marches its slot pixel.  Full: one thread per pixel.
-__global__ void __launch_bounds__(128) march_kernel(const __grid_constant__ MarchArgs a) {
+// Ray -> marched pixel.  Checkerboard: the reference's group grid covers
+// groups_x x groups_y blocks of 4x4 (Renderer.cpp:713-716); each ray is one
+// block's slot pixel.  Full: one ray per pixel.  G consecutive lanes (an
+// aligned segment of a warp) march one ray.
+template <int G>
+__global__ void __launch_bounds__(128, 8) march_kernel(const __grid_constant__ MarchArgs a) {
+    static_assert(G >= 1 && G <= 32 && (32 % G) == 0, "G must divide the warp");
     const Frame F = make_frame(a.params);
     const Tex tx{a.base, a.detail, a.curl, a.weather};
-    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long idx = tid / G;
+    const int lane = (int)(threadIdx.x % G);
+    const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
     Counts cnt{0u, 0u, 0u};
     unsigned pixels = 0;
     int px = 0, py = 0;
@@ -480,96 +601,80 @@ __global__ void __launch_bounds__(128) march_kernel(const __grid_constant__ Marc
         }
     }
     if (active) {
-        march_pixel(a, F, tx, px, py, cnt);
-        pixels = 1;
+        march_pixel<G>(a, F, tx, px, py, cnt, gmask, lane);
+        pixels = lane == 0 ? 1u : 0u;
     }
     if (a.stats) flush_counts(a.stats, cnt, pixels);
 }
 
-// reprojection.comp:193-244 for every pixel the march does not write.
-__global__ void __launch_bounds__(256) reproject_kernel(const __grid_constant__ MarchArgs a) {
-    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int W = a.width, H = a.height;
-    bool active = idx < (long long)W * H;
-    int x = 0, y = 0;
-    if (active) {
-        x = (int)(idx % W);
-        y = (int)(idx / W);
-        const int id = a.time.frame_count_mod16;
-        const int dx = x - a.params.slot_x[id], dy = y - a.params.slot_y[id];
-        const bool marched = dx >= 0 && dy >= 0 && (dx & 3) == 0 && (dy & 3) == 0 && (dx >> 2) < a.groups_x &&
-                             (dy >> 2) < a.groups_y;
-        active = !marched;
-    }
-    if (active) {
-        const mt_params& p = a.params;
-        const Frame F = make_frame(p);
-        float ux = (float)x / (float)W, uy = (float)y / (float)H;
-        f3 eyePos = p.eye_sign * ld3(a.camera.eye);
-        Ray ray = cast_ray(ux, uy, eyePos, a.camera, a.time, a.time.frame_count_mod16, W, H, true);
-        f3 ec = eyePos;
-        ec.y = -F.R;
-        Isect in = ray_sphere(ray.origin, ray.direction, ec, F.Rin);
-        const float* ov = a.camera_old.view;
-        f3 q = in.point;
-        f3 od{ov[0] * q.x + ov[4] * q.y + ov[8] * q.z + ov[12] * 1.0f,
-              ov[1] * q.x + ov[5] * q.y + ov[9] * q.z + ov[13] * 1.0f,
-              ov[2] * q.x + ov[6] * q.y + ov[10] * q.z + ov[14] * 1.0f};
-        od = normalize3(od);
-        od = od / (-od.z);
-        float old_u = (od.x / a.camera.tan_fov_by_2[0]) * 0.5f + 0.5f;
-        float old_v = (od.y / a.camera.tan_fov_by_2[1]) * 0.5f + 0.5f;
-        float mx = old_u - ux, my = old_v - uy;
-        f4v blur{0.0f, 0.0f, 0.0f, 0.0f};
-#pragma unroll
-        for (int i = 0; i < 10; ++i) {
-            float f = (float)i / 10.0f;
-            float iu = roundf((old_u - mx * f) * (float)W);
-            float iv = roundf((old_v - my * f) * (float)H);
-            int ix = imin(imax(f2i(iu), 0), W - 1);
-            int iy = imin(imax(f2i(iv), 0), H - 1);
-            float4 s = __ldg(a.prev + (size_t)iy * (size_t)W + (size_t)ix);
-            blur = blur + f4v{s.x, s.y, s.z, s.w};
-        }
-        blur = blur / 10.0f;
-        a.cur[(size_t)y * (size_t)W + (size_t)x] = make_float4(blur.x, blur.y, blur.z, blur.w);
-    }
-    if (a.stats) {
-        Counts none{0u, 0u, 0u};
-        flush_counts(a.stats, none, active ? 1u : 0u);
-    }
+// Pixels the checkerboard raymarch writes this frame (cloudRayMarch.comp:695-701
+// under the dispatch of Renderer.cpp:713-716).
+MT_HD bool is_marched(const MarchArgs& a, int x, int y) {
+    const int id = a.time.frame_count_mod16;
+    const int dx = x - a.params.slot_x[id], dy = y - a.params.slot_y[id];
+    return dx >= 0 && dy >= 0 && (dx & 3) == 0 && (dy & 3) == 0 && (dx >> 2) < a.groups_x && (dy >> 2) < a.groups_y;
 }
 
-// postProcess_TXAA.frag:223-269, one thread per output pixel (fragment).
-__global__ void __launch_bounds__(256) txaa_kernel(const __grid_constant__ TxaaArgs a) {
-    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int W = a.width, H = a.height;
-    if (idx >= (long long)W * H) return;
-    const int x = (int)(idx % W), y = (int)(idx / W);
-    const mt_params& p = a.params;
-    const Frame F = make_frame(p);
-    float iux = ((float)x + 0.5f) / (float)W, iuy = ((float)y + 0.5f) / (float)H;
-    int ppx = imin(imax(f2i(roundf((float)W * iux)), 0), W - 1);
-    int ppy = imin(imax(f2i(roundf((float)H * iuy)), 0), H - 1);
-    f3 eyePos = p.eye_sign * ld3(a.camera.eye);
-    Ray ray = cast_ray(iux, iuy, eyePos, a.camera, a.time, a.time.frame_count_mod16, W, H, false);
+// The previous camera's uv of the inner-shell hit of a ray
+// (reprojection.comp:205-222, postProcess_TXAA.frag:230-247).
+MT_HD void old_uv(const mt_params& p, const Frame& F, const mt_camera_ubo& cam, const mt_camera_ubo& cam_old,
+                  const mt_time_ubo& tm, float sx, float sy, int W, int H, bool repro, float& old_u, float& old_v) {
+    f3 eyePos = p.eye_sign * ld3(cam.eye);
+    Ray ray = cast_ray(sx, sy, eyePos, cam, tm, tm.frame_count_mod16, W, H, repro);
     f3 ec = eyePos;
     ec.y = -F.R;
     Isect in = ray_sphere(ray.origin, ray.direction, ec, F.Rin);
-    const float* ov = a.camera_old.view;
+    const float* ov = cam_old.view;
     f3 q = in.point;
     f3 od{ov[0] * q.x + ov[4] * q.y + ov[8] * q.z + ov[12] * 1.0f, ov[1] * q.x + ov[5] * q.y + ov[9] * q.z + ov[13] * 1.0f,
           ov[2] * q.x + ov[6] * q.y + ov[10] * q.z + ov[14] * 1.0f};
     od = normalize3(od);
     od = od / (-od.z);
-    float old_u = (od.x / a.camera.tan_fov_by_2[0]) * 0.5f + 0.5f;
-    float old_v = (od.y / a.camera.tan_fov_by_2[1]) * 0.5f + 0.5f;
+    old_u = (od.x / cam.tan_fov_by_2[0]) * 0.5f + 0.5f;
+    old_v = (od.y / cam.tan_fov_by_2[1]) * 0.5f + 0.5f;
+}
 
-    auto load = [&](int i, int j) -> f4v {
-        if (i < 0 || j < 0 || i >= W || j >= H) return f4v{0.0f, 0.0f, 0.0f, 0.0f};
-        float4 s = __ldg(a.current + (size_t)j * (size_t)W + (size_t)i);
-        return f4v{s.x, s.y, s.z, s.w};
-    };
+// reprojection.comp:193-244 for pixel (x, y).
+MT_HD f4v reproject_pixel(const MarchArgs& a, const Frame& F, int x, int y) {
+    const int W = a.width, H = a.height;
+    const float ux = (float)x / (float)W, uy = (float)y / (float)H;
+    float old_u, old_v;
+    old_uv(a.params, F, a.camera, a.camera_old, a.time, ux, uy, W, H, true, old_u, old_v);
+    const float mx = old_u - ux, my = old_v - uy;
+    f4v blur{0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+    for (int i = 0; i < 10; ++i) {
+        const float f = (float)i / 10.0f;
+        const float iu = roundf((old_u - mx * f) * (float)W);
+        const float iv = roundf((old_v - my * f) * (float)H);
+        const int ix = imin(imax(f2i(iu), 0), W - 1);
+        const int iy = imin(imax(f2i(iv), 0), H - 1);
+        const float4 s = __ldg(a.prev + (size_t)iy * (size_t)W + (size_t)ix);
+        blur = blur + f4v{s.x, s.y, s.z, s.w};
+    }
+    return blur / 10.0f;
+}
+
+// The centre pixel of fragment (x, y)'s neighbourhood: pixelPos of
+// postProcess_TXAA.frag:227 with in_uv at the fragment centre.
+MT_HD void txaa_centre(int x, int y, int W, int H, float& iux, float& iuy, int& ppx, int& ppy) {
+    iux = ((float)x + 0.5f) / (float)W;
+    iuy = ((float)y + 0.5f) / (float)H;
+    ppx = imin(imax(f2i(roundf((float)W * iux)), 0), W - 1);
+    ppy = imin(imax(f2i(roundf((float)H * iuy)), 0), H - 1);
+}
+
+// postProcess_TXAA.frag:223-269 for fragment (x, y); `load(i, j)` reads the
+// current frame (0 outside the image, as imageLoad does).
+template <class Load>
+MT_HD f4v txaa_pixel(const mt_params& p, const Frame& F, const mt_camera_ubo& cam, const mt_camera_ubo& cam_old,
+                     const mt_time_ubo& tm, const float4* __restrict__ history, int x, int y, int W, int H,
+                     Load load) {
+    float iux, iuy;
+    int ppx, ppy;
+    txaa_centre(x, y, W, H, iux, iuy, ppx, ppy);
+    float old_u, old_v;
+    old_uv(p, F, cam, cam_old, tm, iux, iuy, W, H, false, old_u, old_v);
     f4v ctl = load(ppx - 1, ppy - 1), ctc = load(ppx, ppy - 1), ctr = load(ppx + 1, ppy - 1);
     f4v cml = load(ppx - 1, ppy), cmc = load(ppx, ppy), cmr = load(ppx + 1, ppy);
     f4v cbl = load(ppx - 1, ppy + 1), cbc = load(ppx, ppy + 1), cbr = load(ppx + 1, ppy + 1);
@@ -582,9 +687,8 @@ __global__ void __launch_bounds__(256) txaa_kernel(const __grid_constant__ TxaaA
     cmin = f4v{0.5f * (cmin.x + cmin5.x), 0.5f * (cmin.y + cmin5.y), 0.5f * (cmin.z + cmin5.z), 0.5f * (cmin.w + cmin5.w)};
     cmax = f4v{0.5f * (cmax.x + cmax5.x), 0.5f * (cmax.y + cmax5.y), 0.5f * (cmax.z + cmax5.z), 0.5f * (cmax.w + cmax5.w)};
     cavg = f4v{0.5f * (cavg.x + cavg5.x), 0.5f * (cavg.y + cavg5.y), 0.5f * (cavg.z + cavg5.z), 0.5f * (cavg.w + cavg5.w)};
-
     f4v curr = cmc;
-    f4v prev = tex2_border(a.history, W, H, old_u, old_v);
+    f4v prev = tex2_border(history, W, H, old_u, old_v);
     // clip_aabb (:171-191)
     f4v pc = min4(max4(cavg, cmin), cmax);
     f3 p_clip{0.5f * (cmax.x + cmin.x), 0.5f * (cmax.y + cmin.y), 0.5f * (cmax.z + cmin.z)};
@@ -600,8 +704,109 @@ __global__ void __launch_bounds__(256) txaa_kernel(const __grid_constant__ TxaaA
     float ud = fabsf(lum0 - lum1) / gmax(lum0, gmax(lum1, 0.2f));
     float uw = 1.0f - ud;
     float k = gmix(p.feedback_min, p.feedback_max, uw * uw);
-    f4v r = mix4(prev, curr, k);
+    return mix4(prev, curr, k);
+}
+
+// reprojection.comp:193-244 for every pixel the march does not write.
+__global__ void __launch_bounds__(256) reproject_kernel(const __grid_constant__ MarchArgs a) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int W = a.width, H = a.height;
+    bool active = idx < (long long)W * H;
+    int x = 0, y = 0;
+    if (active) {
+        x = (int)(idx % W);
+        y = (int)(idx / W);
+        active = !is_marched(a, x, y);
+    }
+    if (active) {
+        const Frame F = make_frame(a.params);
+        const f4v b = reproject_pixel(a, F, x, y);
+        a.cur[(size_t)y * (size_t)W + (size_t)x] = make_float4(b.x, b.y, b.z, b.w);
+    }
+    if (a.stats) {
+        Counts none{0u, 0u, 0u};
+        flush_counts(a.stats, none, active ? 1u : 0u);
+    }
+}
+
+// postProcess_TXAA.frag:223-269, one thread per output pixel (fragment).
+__global__ void __launch_bounds__(256) txaa_kernel(const __grid_constant__ TxaaArgs a) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int W = a.width, H = a.height;
+    if (idx >= (long long)W * H) return;
+    const int x = (int)(idx % W), y = (int)(idx / W);
+    const Frame F = make_frame(a.params);
+    auto load = [&](int i, int j) -> f4v {
+        if (i < 0 || j < 0 || i >= W || j >= H) return f4v{0.0f, 0.0f, 0.0f, 0.0f};
+        float4 s = __ldg(a.current + (size_t)j * (size_t)W + (size_t)i);
+        return f4v{s.x, s.y, s.z, s.w};
+    };
+    const f4v r = txaa_pixel(a.params, F, a.camera, a.camera_old, a.time, a.history, x, y, W, H, load);
     a.out[(size_t)y * (size_t)W + (size_t)x] = make_float4(r.x, r.y, r.z, r.w);
+}
+
+// Reprojection fused with the TXAA resolve, after the raymarch of the frame.
+// A block owns a TW x TH tile of output pixels.  It first builds the current
+// frame over the tile plus the halo its TXAA neighbourhoods reach (one pixel
+// left/up, two right/down: the neighbourhood centre is the fragment's pixel or
+// the next one): marched pixels come from the march's output, the others are
+// reprojected here.  It stores the reprojected pixels it owns (the raw frame
+// the next frame reprojects from), then resolves every owned pixel's TXAA
+// from shared memory.  Values equal those of reproject_kernel + txaa_kernel.
+template <int TW, int TH>
+__global__ void __launch_bounds__(TW * TH) resolve_kernel(const __grid_constant__ MarchArgs a) {
+    constexpr int SW = TW + 3, SH = TH + 3;
+    __shared__ float4 tile[SH][SW];
+    const int W = a.width, H = a.height;
+    const int x0 = blockIdx.x * TW - 1, y0 = blockIdx.y * TH - 1;
+    const Frame F = make_frame(a.params);
+    const bool full = (a.flags & MT_RENDER_FULL) != 0;
+    unsigned reprojected = 0;
+    for (int i = threadIdx.x; i < SW * SH; i += TW * TH) {
+        const int sx = i % SW, sy = i / SW;
+        const int x = x0 + sx, y = y0 + sy;
+        f4v v{0.0f, 0.0f, 0.0f, 0.0f};
+        if (x >= 0 && y >= 0 && x < W && y < H) {
+            const size_t o = (size_t)y * (size_t)W + (size_t)x;
+            if (full || is_marched(a, x, y)) {
+                const float4 c = a.cur[o];
+                v = f4v{c.x, c.y, c.z, c.w};
+            } else {
+                v = reproject_pixel(a, F, x, y);
+                const bool owned = sx >= 1 && sy >= 1 && sx <= TW && sy <= TH;
+                if (owned) {
+                    a.cur[o] = make_float4(v.x, v.y, v.z, v.w);
+                    ++reprojected;
+                }
+            }
+        }
+        tile[sy][sx] = make_float4(v.x, v.y, v.z, v.w);
+    }
+    __syncthreads();
+    const int tx = threadIdx.x % TW, ty = threadIdx.x / TW;
+    const int x = x0 + 1 + tx, y = y0 + 1 + ty;
+    if (x < W && y < H) {
+        auto load = [&](int i, int j) -> f4v {
+            if (i < 0 || j < 0 || i >= W || j >= H) return f4v{0.0f, 0.0f, 0.0f, 0.0f};
+            const float4 s = tile[j - y0][i - x0];
+            return f4v{s.x, s.y, s.z, s.w};
+        };
+        const f4v r = txaa_pixel(a.params, F, a.camera, a.camera_old, a.time, a.history, x, y, W, H, load);
+        a.out[(size_t)y * (size_t)W + (size_t)x] = make_float4(r.x, r.y, r.z, r.w);
+    }
+    if (a.stats) {
+        Counts none{0u, 0u, 0u};
+        flush_counts(a.stats, none, reprojected);
+    }
+}
+
+// rdiv(a, 1/b) against the device's IEEE division, element by element.
+__global__ void selftest_division_kernel(const float* __restrict__ a, const float* __restrict__ b, float* out_rdiv,
+                                         float* out_ieee, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out_rdiv[i] = rdiv(a[i], make_rcp(b[i]));
+    out_ieee[i] = a[i] / b[i];
 }
 
 }  // namespace mt
@@ -610,6 +815,27 @@ __global__ void __launch_bounds__(256) txaa_kernel(const __grid_constant__ TxaaA
 // Launchers (called from the C ABI in mt_capi.cu)
 // ---------------------------------------------------------------------------
 namespace mt {
+
+static cudaError_t launch_march(const MarchArgs& a, cudaStream_t s, const LaunchEvents* ev) {
+    const bool timed = ev && ev->on;
+    const long long m = (a.flags & MT_RENDER_FULL) ? (long long)a.width * a.height
+                                                   : (long long)a.groups_x * a.groups_y;
+    // Images narrower or shorter than 4 pixels give the reference an empty
+    // raymarch dispatch (Renderer.cpp:713-716): nothing is marched.
+    if (timed) cudaEventRecord(ev->march[0], s);
+    if (m > 0) {
+        const int G = a.lanes;
+        const unsigned blocks = (unsigned)((m * G + 127) / 128);
+        switch (G) {
+            case 1: march_kernel<1><<<blocks, 128, 0, s>>>(a); break;
+            case 4: march_kernel<4><<<blocks, 128, 0, s>>>(a); break;
+            case 16: march_kernel<16><<<blocks, 128, 0, s>>>(a); break;
+            default: march_kernel<8><<<blocks, 128, 0, s>>>(a); break;
+        }
+    }
+    if (timed) cudaEventRecord(ev->march[1], s);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_render(const MarchArgs& a, cudaStream_t s, const LaunchEvents* ev) {
     const bool timed = ev && ev->on;
@@ -621,13 +847,41 @@ cudaError_t launch_render(const MarchArgs& a, cudaStream_t s, const LaunchEvents
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
-    const long long m = (a.flags & MT_RENDER_FULL) ? (long long)a.width * a.height
-                                                   : (long long)a.groups_x * a.groups_y;
-    // Images narrower or shorter than 4 pixels give the reference an empty
-    // raymarch dispatch (Renderer.cpp:713-716): nothing is marched.
-    if (timed) cudaEventRecord(ev->march[0], s);
-    if (m > 0) march_kernel<<<(unsigned)((m + 127) / 128), 128, 0, s>>>(a);
-    if (timed) cudaEventRecord(ev->march[1], s);
+    return launch_march(a, s, ev);
+}
+
+constexpr int kResolveTW = 32, kResolveTH = 8;
+
+cudaError_t launch_frame(const MarchArgs& a, cudaStream_t s, const LaunchEvents* ev) {
+    const bool timed = ev && ev->on;
+    if (!a.fused_resolve) {
+        // reprojection, raymarch, TXAA as three launches
+        cudaError_t e = launch_render(a, s, ev);
+        if (e != cudaSuccess) return e;
+        TxaaArgs t;
+        t.camera = a.camera;
+        t.camera_old = a.camera_old;
+        t.time = a.time;
+        t.params = a.params;
+        t.current = a.cur;
+        t.history = a.history;
+        t.out = a.out;
+        t.width = a.width;
+        t.height = a.height;
+        return launch_txaa(t, s, timed ? ev->resolve : nullptr);
+    }
+    cudaError_t e = launch_march(a, s, ev);
+    if (e != cudaSuccess) return e;
+    const dim3 grid((unsigned)((a.width + kResolveTW - 1) / kResolveTW), (unsigned)((a.height + kResolveTH - 1) / kResolveTH));
+    if (timed) cudaEventRecord(ev->resolve[0], s);
+    resolve_kernel<kResolveTW, kResolveTH><<<grid, kResolveTW * kResolveTH, 0, s>>>(a);
+    if (timed) cudaEventRecord(ev->resolve[1], s);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_selftest_division(const float* a, const float* b, float* out_rdiv, float* out_ieee, int n,
+                                     cudaStream_t s) {
+    if (n > 0) selftest_division_kernel<<<(n + 255) / 256, 256, 0, s>>>(a, b, out_rdiv, out_ieee, n);
     return cudaGetLastError();
 }
 

@@ -113,6 +113,14 @@ class Context:
                                        C.byref(params), _ptr(prev), _ptr(cur), _ptr(mask), w, h, flags,
                                        _stream(stream)))
 
+    def render_frame(self, camera, camera_old, time, params, prev, cur, history, out, mask=None,
+                     flags: int = abi.MT_RENDER_CHECKERBOARD, stream=None) -> None:
+        """Raymarch + reprojection + TXAA of one frame in two launches."""
+        h, w = int(cur.shape[0]), int(cur.shape[1])
+        self._check(self.lib.mt_render_frame(self.handle, C.byref(camera), C.byref(camera_old), C.byref(time),
+                                             C.byref(params), _ptr(prev), _ptr(cur), _ptr(history), _ptr(out),
+                                             _ptr(mask), w, h, flags, _stream(stream)))
+
     def txaa(self, camera, camera_old, time, params, current, history, out, stream=None) -> None:
         h, w = int(current.shape[0]), int(current.shape[1])
         self._check(self.lib.mt_txaa(self.handle, C.byref(camera), C.byref(camera_old), C.byref(time),
@@ -122,6 +130,16 @@ class Context:
     def render_batch(self, views: list[abi.View], stream=None) -> None:
         arr = (abi.View * len(views))(*views)
         self._check(self.lib.mt_render_batch(self.handle, arr, len(views), _stream(stream)))
+
+    def set_tuning(self, march_lanes: int | None = None, fused_resolve: bool | None = None) -> abi.Tuning:
+        t = abi.Tuning()
+        self._check(self.lib.mt_get_tuning(self.handle, C.byref(t)))
+        if march_lanes is not None:
+            t.march_lanes = march_lanes
+        if fused_resolve is not None:
+            t.fused_resolve = 1 if fused_resolve else 0
+        self._check(self.lib.mt_set_tuning(self.handle, C.byref(t)))
+        return t
 
     def set_timing(self, enabled: bool) -> None:
         self._check(self.lib.mt_set_timing(self.handle, 1 if enabled else 0))
@@ -172,9 +190,12 @@ class Session:
         marches every pixel: there is no previous frame to reproject), then TXAA."""
         cur, prev = self.raw[self.parity], self.raw[self.parity ^ 1]
         fl = flags if self.frames > 0 else (flags | abi.MT_RENDER_FULL)
-        self.ctx.render(f.camera, f.camera_old, f.time, f.params, prev, cur, self.mask, fl, stream)
-        if self.use_txaa:
-            hist = self.resolved[self.parity ^ 1] if self.frames > 0 else cur
-            self.ctx.txaa(f.camera, f.camera_old, f.time, f.params, cur, hist, self.resolved[self.parity], stream)
+        if self.use_txaa and self.frames > 0:
+            self.ctx.render_frame(f.camera, f.camera_old, f.time, f.params, prev, cur, self.resolved[self.parity ^ 1],
+                                  self.resolved[self.parity], self.mask, fl, stream)
+        else:
+            self.ctx.render(f.camera, f.camera_old, f.time, f.params, prev, cur, self.mask, fl, stream)
+            if self.use_txaa:  # first frame: the frame is its own history
+                self.ctx.txaa(f.camera, f.camera_old, f.time, f.params, cur, cur, self.resolved[self.parity], stream)
         self.parity ^= 1
         self.frames += 1

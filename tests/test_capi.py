@@ -31,7 +31,7 @@ def test_every_declared_function_is_exported(lib):
 def test_struct_layout_matches_header(tmp_path):
     fields = {
         "mt_camera_ubo": abi.CameraUBO, "mt_time_ubo": abi.TimeUBO, "mt_params": abi.Params,
-        "mt_stats": abi.Stats, "mt_view": abi.View,
+        "mt_stats": abi.Stats, "mt_view": abi.View, "mt_tuning": abi.Tuning, "mt_kernel_times": abi.KernelTimes,
     }
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', "int main(void){"]
     for cname, py in fields.items():

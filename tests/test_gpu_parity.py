@@ -228,3 +228,82 @@ def test_argument_errors(ctx, lib):
     assert status(lambda: empty.render(cam, cam, tm, params, b, a, None, 0)) == abi.MT_ERR_NO_VOLUMES
     empty.close()
     torch.cuda.synchronize()
+
+
+@pytest.mark.parametrize("lanes", [1, 4, 16])
+def test_march_lane_counts_give_identical_frames(ctx, lanes):
+    """The step-parallel march is exact: any lane count gives the same bits and counters."""
+    w, h = 320, 180
+    cam, tm, params, _ = scenes.config_view(21, w, h)
+    prev = to_dev(np.random.default_rng(1).random((h, w, 4), dtype=np.float32), torch)
+    outs = []
+    for g in (8, lanes):
+        ctx.set_tuning(march_lanes=g)
+        for flags in (abi.MT_RENDER_FULL, abi.MT_RENDER_CHECKERBOARD):
+            cur = torch.zeros((h, w, 4), dtype=torch.float32, device="cuda")
+            mask = torch.full((h, w), float("nan"), dtype=torch.float32, device="cuda")
+            ctx.render(cam, cam, tm, params, prev, cur, mask, flags | abi.MT_RENDER_COUNT)
+            st = ctx.stats(reset=True)
+            outs.append((cur.cpu().numpy(), mask.cpu().numpy(),
+                         (st.primary_samples, st.light_samples, st.marched_rays, st.pixels)))
+    ctx.set_tuning(march_lanes=0)
+    for a, b in zip(outs[:2], outs[2:]):
+        assert_bits_equal(a[0], b[0], f"lanes {lanes} rgba")
+        assert_bits_equal(a[1], b[1], f"lanes {lanes} mask")
+        assert a[2] == b[2]
+
+
+def test_reciprocal_division_is_ieee_exact(ctx):
+    """The kernels divide by reused denominators through a correctly rounded
+    reciprocal plus one correction step; it must equal IEEE division bit for bit."""
+    rng = np.random.default_rng(123)
+    n = 1 << 22
+    ea = rng.integers(97, 157, n).astype(np.uint32)
+    eb = rng.integers(97, 157, n).astype(np.uint32)
+    ma = rng.integers(0, 1 << 23, n).astype(np.uint32)
+    mb = rng.integers(0, 1 << 23, n).astype(np.uint32)
+    mb[::4] = (1 << 23) - 1
+    mb[1::4] = 0
+    a = ((ea << 23) | ma).view(np.float32) * np.where(rng.random(n) < 0.5, -1, 1).astype(np.float32)
+    b = ((eb << 23) | mb).view(np.float32) * np.where(rng.random(n) < 0.5, -1, 1).astype(np.float32)
+    a[:64] = [0.0, -0.0, 1e-38, -1e-38, 3e38, np.inf, -np.inf, np.nan] * 8
+    b[64:96] = [0.0, -0.0, np.inf, 1e-38] * 8
+    for k in ((0.65, 0.3), (0.85, 0.3), (0.34, 0.07), (1.0, 0.6)):  # widths used by the kernels
+        a[96:4096] = rng.random(4000).astype(np.float32)
+        b[96:4096] = np.float32(k[0]) - np.float32(k[1])
+    da, db = to_dev(a, torch), to_dev(b, torch)
+    r, q = torch.empty_like(da), torch.empty_like(da)
+    st = ctx.lib.mt_selftest_division(ctx.handle, da.data_ptr(), db.data_ptr(), r.data_ptr(), q.data_ptr(), n, None)
+    assert st == abi.MT_OK
+    r, q = r.cpu().numpy(), q.cpu().numpy()
+    with np.errstate(all="ignore"):
+        host = a / b
+    assert_bits_equal(q[~np.isnan(host)], host[~np.isnan(host)], "device IEEE division vs host")
+    assert_bits_equal(r, q, "reciprocal division vs IEEE")
+
+
+@pytest.mark.parametrize("size", [(1, 1), (33, 9), (130, 18), (641, 361), (1920, 1080)])
+def test_fused_frame_equals_render_then_txaa(ctx, size):
+    """mt_render_frame (march + reprojection fused with TXAA) gives exactly the
+    raw frame and the resolved frame of mt_render followed by mt_txaa."""
+    w, h = size
+    cam_old, tm, params, (yaw, pitch) = scenes.config_view(8, w, h)
+    cam = scenes.look((0.0, 100.0, 0.0), yaw + 0.5, pitch, 60.0, w, h)
+    rng = np.random.default_rng(w + h)
+    prev = to_dev(rng.random((h, w, 4), dtype=np.float32), torch)
+    hist = to_dev(rng.random((h, w, 4), dtype=np.float32), torch)
+    for frame, flags in ((3, abi.MT_RENDER_CHECKERBOARD), (11, abi.MT_RENDER_CHECKERBOARD), (0, abi.MT_RENDER_FULL)):
+        tm.frame_count_mod16 = frame
+        cur_a = torch.zeros((h, w, 4), dtype=torch.float32, device="cuda")
+        out_a = torch.zeros_like(cur_a)
+        ctx.render(cam, cam_old, tm, params, prev, cur_a, None, flags)
+        ctx.txaa(cam, cam_old, tm, params, cur_a, hist, out_a)
+        for fused in (False, True):
+            ctx.set_tuning(fused_resolve=fused)
+            cur_b = torch.zeros_like(cur_a)
+            out_b = torch.zeros_like(cur_a)
+            ctx.render_frame(cam, cam_old, tm, params, prev, cur_b, hist, out_b, None, flags)
+            what = f"{w}x{h} frame {frame} fused={fused}"
+            assert_bits_equal(cur_b.cpu().numpy(), cur_a.cpu().numpy(), what + " raw")
+            assert_bits_equal(out_b.cpu().numpy(), out_a.cpu().numpy(), what + " resolved")
+        ctx.set_tuning(fused_resolve=False)
