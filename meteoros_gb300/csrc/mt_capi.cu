@@ -155,18 +155,25 @@ mt_status build_march_args(mt_ctx* ctx, const mt_camera_ubo* cam, const mt_camer
         return fail(ctx, MT_ERR_NO_VOLUMES, "noise volumes have not been uploaded or generated");
     if (p->coverage_mode == 1 && !ctx->weather[p->weather_slot])
         return fail(ctx, MT_ERR_NO_VOLUMES, "weather slot %d holds no weather map", p->weather_slot);
-    if (p->storage != MT_STORAGE_U8)
-        return fail(ctx, MT_ERR_UNSUPPORTED, "storage %d is not available in this build", p->storage);
     std::memset(a, 0, sizeof(*a));
     a->camera = *cam;
     a->camera_old = *cam_old;
     a->time = *tm;
     a->params = *p;
-    a->base = ctx->base;
-    a->detail = ctx->detail;
-    a->curl = ctx->curl;
-    a->weather = ctx->weather[p->weather_slot] ? ctx->weather[p->weather_slot] : ctx->curl;
-    if (p->coverage_mode == 0) a->weather = ctx->curl;  // never read
+    const int k = p->storage == MT_STORAGE_BF16 ? 1 : 0;
+    const uint32_t* weather8 = (p->coverage_mode == 1) ? ctx->weather[p->weather_slot] : ctx->curl;
+    const uint2* weather16 = (p->coverage_mode == 1) ? ctx->weather16[k][p->weather_slot] : ctx->curl16[k];
+    if (p->storage == MT_STORAGE_U8) {
+        a->vol[0] = ctx->base;
+        a->vol[1] = ctx->detail;
+        a->vol[2] = ctx->curl;
+        a->vol[3] = weather8;  // never read when coverage_mode == 0
+    } else {
+        a->vol[0] = ctx->base16[k];
+        a->vol[1] = ctx->detail16[k];
+        a->vol[2] = ctx->curl16[k];
+        a->vol[3] = weather16;
+    }
     a->prev = (const float4*)prev;
     a->cur = (float4*)cur;
     a->mask = mask;

@@ -14,6 +14,8 @@
 //   round = half away from zero; float->int truncates and saturates (NaN -> 0).
 #pragma once
 #include <cstdint>
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "../../include/meteoros.h"
@@ -72,7 +74,7 @@ struct Rcp {
 };
 // The IEEE division, out of line: one shared copy keeps the callers small in
 // the instruction cache (the march loop is instruction-fetch bound otherwise).
-__device__ __noinline__ float div_ieee(float a, float b) { return a / b; }
+static __device__ __noinline__ float div_ieee(float a, float b) { return a / b; }
 MT_HD Rcp make_rcp(float b) { return Rcp{b, div_ieee(1.0f, b)}; }
 MT_HD float rdiv(float a, Rcp r) {
     const float q0 = __fmul_rn(a, r.y);
@@ -82,7 +84,7 @@ MT_HD float rdiv(float a, Rcp r) {
     if (aq >= 0x1p-100f && aq <= 0x1p100f) return q;
     return div_ieee(a, r.b);
 }
-__device__ __noinline__ float pow_nl(float x, float y) { return powf(x, y); }
+static __device__ __noinline__ float pow_nl(float x, float y) { return powf(x, y); }
 
 MT_HD float dot3(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 MT_HD float length3(f3 a) { return sqrtf(dot3(a, a)); }
@@ -170,6 +172,70 @@ template <int N> MT_HD f4v tex2_u8(const uint32_t* __restrict__ img, float sx, f
     f4v c0 = lerp_texels(__ldg(img + y0 * N + x0), __ldg(img + y0 * N + x1), a);
     f4v c1 = lerp_texels(__ldg(img + y1 * N + x0), __ldg(img + y1 * N + x1), a);
     return lerp4(c0, c1, b) * (1.0f / 255.0f);
+}
+
+// ---------------------------------------------------------------------------
+// Precision-form samplers: texels stored as four 16-bit values (uint2 =
+// (r,g),(b,a) pairs, IEEE half or bfloat16), interpolated as packed pairs
+// (half2 / bfloat16x2 fused multiply-adds), the weights rounded to the pair
+// type.  The index arithmetic is the FP32 one above.  Results are returned
+// in FP32; the precision form is measured against the FP64 oracle.
+// ---------------------------------------------------------------------------
+template <class P> struct Pair;
+template <> struct Pair<__half2> {
+    static MT_HD __half2 from_bits(uint32_t u) { return *reinterpret_cast<__half2*>(&u); }
+    static MT_HD __half2 splat(float f) { return __float2half2_rn(f); }
+    static MT_HD float2 to_float2(__half2 h) { return __half22float2(h); }
+};
+template <> struct Pair<__nv_bfloat162> {
+    static MT_HD __nv_bfloat162 from_bits(uint32_t u) { return *reinterpret_cast<__nv_bfloat162*>(&u); }
+    static MT_HD __nv_bfloat162 splat(float f) { return __float2bfloat162_rn(f); }
+    static MT_HD float2 to_float2(__nv_bfloat162 h) { return __bfloat1622float2(h); }
+};
+
+template <class P> struct PairTexel {
+    P rg, ba;
+};
+template <class P> MT_HD PairTexel<P> ld_pair(const uint2* __restrict__ p) {
+    const uint2 v = __ldg(p);
+    return PairTexel<P>{Pair<P>::from_bits(v.x), Pair<P>::from_bits(v.y)};
+}
+template <class P> MT_HD PairTexel<P> lerp_pair(PairTexel<P> p, PairTexel<P> q, P t) {
+    return PairTexel<P>{__hfma2(t, __hsub2(q.rg, p.rg), p.rg), __hfma2(t, __hsub2(q.ba, p.ba), p.ba)};
+}
+template <class P> MT_HD f4v pair_to_f4(PairTexel<P> c) {
+    const float2 rg = Pair<P>::to_float2(c.rg), ba = Pair<P>::to_float2(c.ba);
+    return f4v{rg.x, rg.y, ba.x, ba.y};
+}
+
+template <int N, class P> MT_HD f4v tex3_p16(const uint2* __restrict__ vol, f3 s) {
+    constexpr unsigned M = (unsigned)N - 1u;
+    const float fn = (float)N;
+    float u = s.x * fn - 0.5f, v = s.y * fn - 0.5f, w = s.z * fn - 0.5f;
+    float fu = floorf(u), fv = floorf(v), fw = floorf(w);
+    const P a = Pair<P>::splat(u - fu), b = Pair<P>::splat(v - fv), g = Pair<P>::splat(w - fw);
+    unsigned iu = (unsigned)f2i(fu), iv = (unsigned)f2i(fv), iw = (unsigned)f2i(fw);
+    unsigned x0 = iu & M, x1 = (iu + 1u) & M, y0 = iv & M, y1 = (iv + 1u) & M, z0 = iw & M, z1 = (iw + 1u) & M;
+    const uint2* p0 = vol + (size_t)z0 * (N * N);
+    const uint2* p1 = vol + (size_t)z1 * (N * N);
+    PairTexel<P> c00 = lerp_pair(ld_pair<P>(p0 + y0 * N + x0), ld_pair<P>(p0 + y0 * N + x1), a);
+    PairTexel<P> c10 = lerp_pair(ld_pair<P>(p0 + y1 * N + x0), ld_pair<P>(p0 + y1 * N + x1), a);
+    PairTexel<P> c01 = lerp_pair(ld_pair<P>(p1 + y0 * N + x0), ld_pair<P>(p1 + y0 * N + x1), a);
+    PairTexel<P> c11 = lerp_pair(ld_pair<P>(p1 + y1 * N + x0), ld_pair<P>(p1 + y1 * N + x1), a);
+    return pair_to_f4(lerp_pair(lerp_pair(c00, c10, b), lerp_pair(c01, c11, b), g));
+}
+
+template <int N, class P> MT_HD f4v tex2_p16(const uint2* __restrict__ img, float sx, float sy) {
+    constexpr unsigned M = (unsigned)N - 1u;
+    const float fn = (float)N;
+    float u = sx * fn - 0.5f, v = sy * fn - 0.5f;
+    float fu = floorf(u), fv = floorf(v);
+    const P a = Pair<P>::splat(u - fu), b = Pair<P>::splat(v - fv);
+    unsigned iu = (unsigned)f2i(fu), iv = (unsigned)f2i(fv);
+    unsigned x0 = iu & M, x1 = (iu + 1u) & M, y0 = iv & M, y1 = (iv + 1u) & M;
+    PairTexel<P> c0 = lerp_pair(ld_pair<P>(img + y0 * N + x0), ld_pair<P>(img + y0 * N + x1), a);
+    PairTexel<P> c1 = lerp_pair(ld_pair<P>(img + y1 * N + x0), ld_pair<P>(img + y1 * N + x1), a);
+    return pair_to_f4(lerp_pair(c0, c1, b));
 }
 
 // Bilinear sample of an RGBA32F frame with CLAMP_TO_BORDER, opaque black

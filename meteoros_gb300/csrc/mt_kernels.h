@@ -15,10 +15,10 @@ struct MarchArgs {
     mt_camera_ubo camera_old;
     mt_time_ubo time;
     mt_params params;
-    const uint32_t* base;     // MT_BASE_N^3 RGBA8 words
-    const uint32_t* detail;   // MT_DETAIL_N^3 RGBA8 words
-    const uint32_t* curl;     // MT_CURL_N^2 RGBA8 words
-    const uint32_t* weather;  // MT_WEATHER_N^2 RGBA8 words (slot params.weather_slot)
+    // base (MT_BASE_N^3), detail (MT_DETAIL_N^3), curl (MT_CURL_N^2), weather
+    // (MT_WEATHER_N^2, slot params.weather_slot) in params.storage: RGBA8
+    // words (uint32_t) or four 16-bit values (uint2)
+    const void* vol[4];
     const float4* prev;
     float4* cur;
     float* mask;
@@ -59,6 +59,9 @@ struct LaunchEvents {
 };
 
 cudaError_t launch_render(const MarchArgs& a, cudaStream_t s, const LaunchEvents* ev);
+cudaError_t launch_march_u8(const MarchArgs& a, cudaStream_t s, long long rays);
+cudaError_t launch_march_f16(const MarchArgs& a, cudaStream_t s, long long rays);
+cudaError_t launch_march_bf16(const MarchArgs& a, cudaStream_t s, long long rays);
 cudaError_t launch_txaa(const TxaaArgs& a, cudaStream_t s, const cudaEvent_t* ev);
 // The raymarch, then reprojection fused with TXAA (a.history -> a.out).
 cudaError_t launch_frame(const MarchArgs& a, cudaStream_t s, const LaunchEvents* ev);

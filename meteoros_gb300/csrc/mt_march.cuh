@@ -1,0 +1,358 @@
+// The raymarch kernel (cloudRayMarch.comp:565-826), templated on the lanes
+// per ray and on the storage of the noise volumes:
+//   MT_STORAGE_U8    RGBA8 volumes, exact FP32 filtering (the plain form)
+//   MT_STORAGE_F16   IEEE half volumes, half2 interpolation (precision form)
+//   MT_STORAGE_BF16  bfloat16 volumes, bfloat16x2 interpolation
+// Everything after the filtered texel (FBM, remaps, erosion, lighting,
+// accumulation) is FP32 in all three.  Each storage is instantiated by its own
+// translation unit (mt_march_u8.cu, mt_march_f16.cu, mt_march_bf16.cu).
+#pragma once
+#include "mt_shared.cuh"
+
+namespace mt {
+
+// Storage-specific volume access.
+template <int S> struct Vol;
+template <> struct Vol<MT_STORAGE_U8> {
+    using T = uint32_t;
+    template <int N> static MT_HD f4v tex3(const T* v, f3 s) { return tex3_u8<N>(v, s); }
+    template <int N> static MT_HD f4v tex2(const T* v, float x, float y) { return tex2_u8<N>(v, x, y); }
+};
+template <> struct Vol<MT_STORAGE_F16> {
+    using T = uint2;
+    template <int N> static MT_HD f4v tex3(const T* v, f3 s) { return tex3_p16<N, __half2>(v, s); }
+    template <int N> static MT_HD f4v tex2(const T* v, float x, float y) { return tex2_p16<N, __half2>(v, x, y); }
+};
+template <> struct Vol<MT_STORAGE_BF16> {
+    using T = uint2;
+    template <int N> static MT_HD f4v tex3(const T* v, f3 s) { return tex3_p16<N, __nv_bfloat162>(v, s); }
+    template <int N> static MT_HD f4v tex2(const T* v, float x, float y) {
+        return tex2_p16<N, __nv_bfloat162>(v, x, y);
+    }
+};
+
+struct Weather {
+    float lo, mul, type;
+    float hgrad;  // height gradient at the primary sample, shared by its light samples
+    Rcp r_lo;     // 1 - lo, the coverage remap's width, shared by the step's samples
+};
+
+template <int S> struct Tex {
+    const typename Vol<S>::T* base;
+    const typename Vol<S>::T* detail;
+    const typename Vol<S>::T* curl;
+    const typename Vol<S>::T* weather;
+};
+
+template <int S> MT_HD Weather weather_at(const mt_params& p, const Frame& F, const Tex<S>& tx, f3 pos, f3 ec) {
+    Weather w;
+    w.hgrad = 1.0f;
+    if (p.coverage_mode == 0) {
+        w.lo = p.coverage;
+        w.mul = p.coverage;
+        w.type = 0.0f;
+    } else {
+        f4v wd = Vol<S>::template tex2<MT_WEATHER_N>(tx.weather, rdiv(pos.x - ec.x, F.r_weather), rdiv(pos.z - ec.z, F.r_weather));
+        w.lo = 1.0f - wd.x;
+        w.mul = wd.x;
+        w.type = wd.z;
+    }
+    w.r_lo = make_rcp(1.0f - w.lo);
+    return w;
+}
+
+// cloudRayMarch.comp:499-540
+template <int S>
+MT_HD float sample_low_frequency(const mt_params& p, const Tex<S>& tx, f3 point, float relH, const Weather& wt) {
+    f4v n = Vol<S>::template tex3<MT_BASE_N>(tx.base, point);
+    float fbm = (n.y * 0.625f) + (n.z * 0.25f) + (n.w * 0.125f);
+    fbm = gclamp(fbm, 0.0f, 1.0f);
+    float baseCloud = remap_clamped(n.x, (fbm - 0.9f), 1.0f, 0.0f, 1.0f);
+    // getDensityHeightGradientForPoint(relH, type): every call of a step passes
+    // the primary sample's height and weather, so it is evaluated once per step
+    // (Weather::hgrad).
+    if (p.height_gradient) baseCloud = baseCloud * wt.hgrad;
+    // remapClampedBeforeAndAfter(baseCloud, lo, 1, 0, 1) with its width 1 - lo
+    // shared by the step's samples
+    float v = gclamp(baseCloud, wt.lo, 1.0f);
+    float bc = gclamp(0.0f + ((rdiv(v - wt.lo, wt.r_lo)) * (1.0f - 0.0f)), 0.0f, 1.0f);
+    return bc * wt.mul;
+}
+
+// cloudRayMarch.comp:542-563.  The texture part is the same for the primary
+// erosion (:645) and the six cone-light erosions (:665): all are evaluated at
+// the primary sample point with the primary height, so it is computed once.
+template <int S> MT_HD float erosion_modifier(const Tex<S>& tx, f3 point, float h) {
+    f4v curl = Vol<S>::template tex2<MT_CURL_N>(tx.curl, point.x, point.y);
+    point.x = point.x + (curl.x * (1.0f - h)) * 0.5f;
+    point.y = point.y + (curl.y * (1.0f - h)) * 0.5f;
+    f4v hf = Vol<S>::template tex3<MT_DETAIL_N>(tx.detail, point);
+    float hfbm = (hf.x * 0.625f) + (hf.y * 0.25f) + (hf.z * 0.125f);
+    return gclamp(gmix(hfbm, 1.0f - hfbm, gclamp(h * 2.0f, 0.0f, 1.0f)), 0.0f, 1.0f);
+}
+// Per-ray constants of cloudRayMarch.comp:565-624, shared by every step.
+struct RayConsts {
+    Ray ray;
+    f3 ec, startPos;
+    f3 kernel[6];
+    f3 wind, skew;
+    float stepSize, cos_angle, cos_q, HG_light, total_time;
+    int pixelID;
+};
+
+static __device__ __noinline__ void ray_consts(const mt_params& p, const mt_time_ubo& tm, const Ray& ray, f3 ec,
+                                        f3 startPos, float stepSize, int pixelID, RayConsts& rc) {
+    rc.ray = ray;
+    rc.ec = ec;
+    rc.startPos = startPos;
+    rc.stepSize = stepSize;
+    rc.pixelID = pixelID;
+    const f3 lightDir = normalize3(ld3(p.sun_light_pos) - ray.origin);
+    rc.cos_angle = dot3(normalize3(ray.direction), lightDir);
+    rc.cos_q = (rc.cos_angle - 0.7f) / (1.0f - 0.7f);
+    rc.HG_light = gmax(henyey_greenstein(rc.cos_angle, 0.6f), 0.7f * henyey_greenstein(rc.cos_angle, 0.99f - 0.1f));
+    float ax = fabsf(lightDir.x), ay = fabsf(lightDir.y), az = fabsf(lightDir.z);
+    f3 maxComp;
+    if (ax > ay && ax > az)
+        maxComp = f3{ax, 0.0f, 0.0f};
+    else if (ay > ax && ay > az)
+        maxComp = f3{0.0f, ay, 0.0f};
+    else
+        maxComp = f3{0.0f, 0.0f, az};
+    f3 zC = cross3(lightDir, maxComp);
+    f3 xC = cross3(zC, lightDir);
+    rc.kernel[0] = mat3mul(xC, lightDir, zC, f3{0.1f, 0.25f, -0.15f});
+    rc.kernel[1] = mat3mul(xC, lightDir, zC, f3{0.2f, 0.5f, 0.2f});
+    rc.kernel[2] = mat3mul(xC, lightDir, zC, f3{-0.2f, 0.1f, -0.1f});
+    rc.kernel[3] = mat3mul(xC, lightDir, zC, f3{-0.05f, 0.75f, 0.05f});
+    rc.kernel[4] = mat3mul(xC, lightDir, zC, f3{-0.1f, 1.0f, 0.0f});
+    rc.kernel[5] = mat3mul(xC, lightDir, zC, f3{0.0f, 3.0f, 0.0f});
+    rc.wind = ld3(p.wind_dir) * p.wind_speed;
+    rc.skew = ld3(p.skew_dir);
+    rc.total_time = tm.time[1];
+}
+
+struct StepOut {
+    int in_cloud;  // baseDensity > 0 (cloudRayMarch.comp:642)
+    float hfd;     // eroded density (:645)
+    float E;       // light energy (:673)
+};
+
+// One iteration of the march loop body (cloudRayMarch.comp:629-678) at
+// parameter t, up to the accumulation: everything that does not depend on the
+// running accumDensity / transmittance.
+template <int S>
+MT_HD StepOut eval_step(const mt_params& p, const Frame& F, const Tex<S>& tx, const mt_time_ubo& tm,
+                        const RayConsts& rc, float t) {
+    StepOut o{0, 0.0f, 0.0f};
+    int _index = f2i(gmod((float)(rc.pixelID + f2i(t)), 16.0f));
+    float jx, jy;
+    jitter_offset(tm, _index, 1.0f, 1.0f, false, jx, jy);  // halton values; / 75 below
+    jx = rdiv(jx, MT_RCP(0.0f, 75.0f));
+    jy = rdiv(jy, MT_RCP(0.0f, 75.0f));
+    f3 jd = rc.ray.direction + f3{jx, (jx + jy) * 1.180f, jy};
+    f3 pos = rc.ray.origin + t * jd;
+    f3 sp = relative_position(F, pos, rc.ec);
+    sp = f3{rdiv(sp.x, F.r_period), rdiv(sp.y, F.r_period), rdiv(sp.z, F.r_period)};
+    float relH = relative_height(F, pos, rc.ec, rc.startPos, rc.ray.direction, rc.ray.origin);
+    sp = sp + ((relH * rc.skew) * p.cloud_top_offset) * 0.009f;
+    sp = sp + rc.wind * rc.total_time;
+    Weather wt = weather_at<S>(p, F, tx, pos, rc.ec);
+    if (p.height_gradient) wt.hgrad = height_gradient(relH, wt.type);
+    float baseDensity = sample_low_frequency<S>(p, tx, sp, relH, wt) * 0.380f;
+    if (baseDensity > 0.0f) {
+        const Erosion ero = make_erosion(erosion_modifier<S>(tx, sp, relH));
+        o.in_cloud = 1;
+        o.hfd = erode(baseDensity * 1.4f, ero);
+        float dl = 0.0f;
+        // Kept rolled: six inlined copies of the sampler overflow the
+        // instruction cache (the dominant stall when unrolled).
+#pragma unroll 1
+        for (int i = 0; i < 6; ++i) {
+            f3 lightPos = pos + ((rc.stepSize * rc.kernel[i]) * (float)i);
+            f3 slp = relative_position(F, lightPos, rc.ec);
+            float cbl = sample_low_frequency<S>(p, tx, slp, relH, wt);
+            if (cbl > 0.0f) dl = dl + erode(1.5f * cbl, ero);
+        }
+        o.E = light_energy(relH, dl, baseDensity, rc.HG_light, rc.cos_q, 5.0f);
+    }
+    return o;
+}
+
+// cloudRayMarch.comp:565-688, step-parallel.  A group of G lanes marches one
+// ray: lane j evaluates step c*G + j of chunk c, with t rebuilt by the same
+// serial `t += stepSize` additions as the reference's loop, so every lane sees
+// bit-identical t.  The loop-carried part (accumDensity, transmittance,
+// colour, the early exit) is then applied in step order by an in-group scan;
+// steps past the exit are discarded.  Result, counters and control flow equal
+// the sequential loop's.
+template <int G, int S>
+MT_HD f3 ray_march_group(const mt_params& p, const Frame& F, const Tex<S>& tx, const mt_time_ubo& tm, const Ray& ray,
+                         f3 ec, f3 startPos, float start_t, float end_t, int pixelID, float& accum, Counts& cnt,
+                         unsigned gmask, int lane) {
+    float _dot = dot3(ray.direction, f3{0.0f, 1.0f, 0.0f});
+    float maxSteps;
+    if (p.steps_min == p.steps_max)
+        maxSteps = (float)p.steps_min;
+    else
+        maxSteps = floorf(gmix((float)p.steps_min, (float)p.steps_max, 1.0f - _dot));
+    const float thick = end_t - start_t;
+    const float stepSize = thick / maxSteps;
+    RayConsts rc;
+    ray_consts(p, tm, ray, ec, startPos, stepSize, pixelID, rc);
+    float transmittance = 1.0f;
+    f3 color{0.0f, 0.0f, 0.0f};
+    // Iteration guard (not in the reference): a step below the ulp of t would
+    // never advance.  A valid ray runs steps or steps+1 iterations.
+    const int cap = 2 * f2i(maxSteps) + 8;
+    if (lane == 0) cnt.rays++;
+    float t_base = start_t;
+    int s_base = 0;
+    bool done = false;
+    while (!done) {
+        float t = t_base;
+        for (int k = 0; k < lane; ++k) t += stepSize;
+        const int valid = (t < end_t) && (s_base + lane < cap);
+        StepOut o{0, 0.0f, 0.0f};
+        if (valid) o = eval_step<S>(p, F, tx, tm, rc, t);
+#pragma unroll
+        for (int k = 0; k < G; ++k) {
+            if (!__shfl_sync(gmask, valid, k, G)) {
+                done = true;
+                break;
+            }
+            const int in_cloud = __shfl_sync(gmask, o.in_cloud, k, G);
+            const float hfd = __shfl_sync(gmask, o.hfd, k, G);
+            const float E = __shfl_sync(gmask, o.E, k, G);
+            if (lane == 0) cnt.primary++;
+            if (in_cloud) {
+                accum = accum + hfd * 0.5f;
+                transmittance = gmix(transmittance, E, (1.0f - accum));
+                color = color + f3{transmittance, transmittance, transmittance};
+                if (lane == 0) cnt.light += 6;
+            }
+            if (accum >= p.accum_limit) {
+                accum = 1.0f;
+                done = true;
+                break;
+            }
+        }
+        if (!done) {
+            t_base = __shfl_sync(gmask, t, G - 1, G) + stepSize;
+            s_base += G;
+        }
+    }
+    return color;
+}
+
+// cloudRayMarch.comp:690-826 for one pixel, marched by a group of G lanes;
+// lane 0 stores.
+template <int G, int S>
+MT_HD void march_pixel(const MarchArgs& a, const Frame& F, const Tex<S>& tx, int px, int py, Counts& cnt,
+                       unsigned gmask, int lane) {
+    const mt_params& p = a.params;
+    const int W = a.width, H = a.height;
+    const int pixelID = a.time.frame_count_mod16;
+    float ux = (float)px / (float)W, uy = (float)py / (float)H;
+    uy = 1.0f - uy;
+    f3 eyePos = p.eye_sign * ld3(a.camera.eye);
+    Ray ray = cast_ray(ux, uy, eyePos, a.camera, a.time, pixelID, W, H, false);
+    const float sunIntensity = 0.780f;
+    float _dot = dot3(f3{0.0f, 1.0f, 0.0f}, ray.direction);
+    const float bgMul = gmax(0.620f, _dot);
+    const float fade = 0.06f;
+    const size_t o = (size_t)py * (size_t)W + (size_t)px;
+    f3 bg;
+    if (_dot < 0.0f) {
+        f3 cNear = f3{0.0f, 0.16f, 0.51f} * 0.4f;
+        f3 c2 = f3{0.0f, 0.73f, 0.95f} * 0.5f;
+        bg = mix3(cNear, c2, -ray.direction.y * 5.5f);
+        if (lane == 0) {
+            a.cur[o] = make_float4(bg.x, bg.y, bg.z, 1.0f);
+            if (a.mask) a.mask[o] = 0.0f;
+        }
+        return;
+    }
+    bg = atmosphere_color(p, ray.direction, ld3(p.sky_sun_pos) - ray.origin, sunIntensity);
+    bg = bg * bgMul;
+    if (_dot < fade) {
+        if (lane == 0) {
+            a.cur[o] = make_float4(bg.x, bg.y, bg.z, 1.0f);
+            if (a.mask) a.mask[o] = 0.0f;
+        }
+        return;
+    }
+    f3 ec = eyePos;
+    ec.y = -F.R;
+    Isect in, out;
+    if (p.fp64_shells) {
+        in = ray_sphere_fp64(ray.origin, ray.direction, ec, F.Rin);
+        out = ray_sphere_fp64(ray.origin, ray.direction, ec, F.Rout);
+    } else {
+        in = ray_sphere(ray.origin, ray.direction, ec, F.Rin);
+        out = ray_sphere(ray.origin, ray.direction, ec, F.Rout);
+    }
+    float accum = 0.0f;
+    f3 res = ray_march_group<G, S>(p, F, tx, a.time, ray, ec, in.point, in.t, out.t, pixelID, accum, cnt, gmask, lane);
+    if (lane != 0) return;
+    float godAccum = accum;
+    accum = accum * gsmoothstep(0.0f, 1.0f, gmin(1.0f, remap(ray.direction.y, fade, 0.2f, 0.0f, 1.0f)));
+    f3 fc = mix3(bg, res, accum);
+    a.cur[o] = make_float4(fc.x, fc.y, fc.z, 1.0f);
+    if (a.mask) a.mask[o] = godray_value(25.0f * gmin(0.05f, 1.0f - godAccum), ray.direction.y);
+}
+
+// Ray -> marched pixel.  Checkerboard: the reference's group grid covers
+// groups_x x groups_y blocks of 4x4 (Renderer.cpp:713-716); each ray is one
+// block's slot pixel.  Full: one ray per pixel.  G consecutive lanes (an
+// aligned segment of a warp) march one ray.
+template <int G, int S>
+__global__ void __launch_bounds__(128, 8) march_kernel(const __grid_constant__ MarchArgs a) {
+    static_assert(G >= 1 && G <= 32 && (32 % G) == 0, "G must divide the warp");
+    const Frame F = make_frame(a.params);
+    using T = typename Vol<S>::T;
+    const Tex<S> tx{(const T*)a.vol[0], (const T*)a.vol[1], (const T*)a.vol[2], (const T*)a.vol[3]};
+    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long idx = tid / G;
+    const int lane = (int)(threadIdx.x % G);
+    const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
+    Counts cnt{0u, 0u, 0u};
+    unsigned pixels = 0;
+    int px = 0, py = 0;
+    bool active;
+    if (a.flags & MT_RENDER_FULL) {
+        active = idx < (long long)a.width * a.height;
+        if (active) {
+            px = (int)(idx % a.width);
+            py = (int)(idx / a.width);
+        }
+    } else {
+        active = idx < (long long)a.groups_x * a.groups_y;
+        if (active) {
+            const int id = a.time.frame_count_mod16;
+            px = (int)(idx % a.groups_x) * 4 + a.params.slot_x[id];
+            py = (int)(idx / a.groups_x) * 4 + a.params.slot_y[id];
+            active = px < a.width && py < a.height;
+        }
+    }
+    if (active) {
+        march_pixel<G, S>(a, F, tx, px, py, cnt, gmask, lane);
+        pixels = lane == 0 ? 1u : 0u;
+    }
+    if (a.stats) flush_counts(a.stats, cnt, pixels);
+}
+
+
+template <int S> cudaError_t launch_march_storage(const MarchArgs& a, cudaStream_t s, long long rays) {
+    const int G = a.lanes;
+    const unsigned blocks = (unsigned)((rays * G + 127) / 128);
+    switch (G) {
+        case 1: march_kernel<1, S><<<blocks, 128, 0, s>>>(a); break;
+        case 4: march_kernel<4, S><<<blocks, 128, 0, s>>>(a); break;
+        case 16: march_kernel<16, S><<<blocks, 128, 0, s>>>(a); break;
+        default: march_kernel<8, S><<<blocks, 128, 0, s>>>(a); break;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace mt

@@ -1,4 +1,5 @@
-// Raymarch, reprojection and TXAA kernels of the compute stage (FP32 form).
+// Reprojection and TXAA kernels of the compute stage, and the launchers of
+// every render kernel (the raymarch itself lives in mt_march.cuh).
 //
 //   march_kernel        <- shaders/cloudRayMarch.comp:690-826 (one thread per
 //                          marched pixel)
@@ -16,596 +17,9 @@
 // Compiled with -fmad=false: see mt_device.cuh.
 #include <cuda_runtime.h>
 
-#include "mt_device.cuh"
-#include "mt_kernels.h"
+#include "mt_shared.cuh"
 
 namespace mt {
-
-struct Frame {
-    float R, Rin, Rout, thickness, inner_alt;
-    Rcp r_thick, r_period, r_weather;  // per-frame denominators (see rdiv)
-};
-
-MT_HD Frame make_frame(const mt_params& p) {
-    Frame F;
-    F.R = p.earth_radius;
-    F.Rin = p.shell_inner_radius;
-    F.Rout = p.shell_outer_radius;
-    F.thickness = F.Rout - F.Rin;
-    F.inner_alt = F.Rin - F.R;
-    F.r_thick = make_rcp(F.thickness);
-    F.r_period = make_rcp(p.noise_period);
-    F.r_weather = make_rcp(p.weather_scale);
-    return F;
-}
-
-// remap() whose range width omax - omin is known ahead: the quotient through
-// the correctly rounded reciprocal of that width (rdiv).
-MT_HD float remap_r(float v, float omin, Rcp width, float nmin, float nmax) {
-    return nmin + ((rdiv(v - omin, width)) * (nmax - nmin));
-}
-// The reciprocal of a compile-time width, rounded once by the compiler.
-#define MT_RCP(omin, omax) (Rcp{(omax) - (omin), 1.0f / ((omax) - (omin))})
-
-struct Ray {
-    f3 origin, direction;
-};
-struct Isect {
-    f3 point;
-    bool valid;
-    float t;
-};
-
-// cloudRayMarch.comp:114-132; reprojection.comp:72-90 reads halton 1/2 again
-// for index >= 4 (`repro`).
-MT_HD void jitter_offset(const mt_time_ubo& tm, int index, float dimx, float dimy, bool repro, float& jx,
-                         float& jy) {
-    index = index / 2;
-    float x, y;
-    if (index < 4) {
-        x = tm.halton_seq1[index];
-        y = tm.halton_seq2[index];
-    } else {
-        index -= 4;
-        if (repro) {
-            x = tm.halton_seq1[index];
-            y = tm.halton_seq2[index];
-        } else {
-            x = tm.halton_seq3[index];
-            y = tm.halton_seq4[index];
-        }
-    }
-    jx = x / dimx;
-    jy = y / dimy;
-}
-
-// cloudRayMarch.comp:194-226
-MT_HD Ray cast_ray(float sx, float sy, f3 eye, const mt_camera_ubo& cam, const mt_time_ubo& tm, int pixelID, int W,
-                   int H, bool repro) {
-    const float* v = cam.view;
-    f3 camRight = normalize3(f3{v[0], v[4], v[8]});
-    f3 camUp = normalize3(f3{v[1], v[5], v[9]});
-    f3 camLook = -normalize3(f3{v[2], v[6], v[10]});
-    float nx = sx * 2.0f - 1.0f, ny = sy * 2.0f - 1.0f;
-    float jx, jy;
-    jitter_offset(tm, pixelID, (float)W, (float)H, repro, jx, jy);
-    nx = nx + jx;
-    ny = ny + jy;
-    f3 cam_x = (nx * cam.tan_fov_by_2[0]) * camRight;
-    f3 cam_y = (ny * cam.tan_fov_by_2[1]) * camUp;
-    f3 ref = eye + camLook;
-    f3 pp = ref + cam_x + cam_y;
-    return Ray{eye, normalize3(pp - eye)};
-}
-
-// cloudRayMarch.comp:229-273 (t = length(p - rO) with the normalised rO, as
-// the reference defines it).
-MT_HD Isect ray_sphere(f3 rO, f3 rD, f3 c, float radius) {
-    Isect is;
-    is.valid = false;
-    is.point = f3{0.0f, 0.0f, 0.0f};
-    is.t = 0.0f;
-    rO = rO - c;
-    rO = rO / radius;
-    float A = dot3(rD, rD);
-    float B = 2.0f * dot3(rD, rO);
-    float C = dot3(rO, rO) - 1.0f;
-    float disc = B * B - 4.0f * A * C;
-    if (disc < 0.0f) return is;
-    float t = (-B - sqrtf(disc)) / (2.0f * A);
-    if (t < 0.0f) t = (-B + sqrtf(disc)) / (2.0f * A);
-    if (t >= 0.0f) {
-        f3 pnt = rO + t * rD;
-        is.valid = true;
-        pnt = pnt * radius;
-        pnt = pnt + c;
-        is.point = pnt;
-        is.t = length3(pnt - rO);
-    }
-    return is;
-}
-
-// The same intersection in FP64 (precision form): the normalised-sphere
-// quadratic cancels badly in FP32 (C = |rO|^2 - 1 with |rO| ~ 1).
-MT_HD Isect ray_sphere_fp64(f3 rOf, f3 rDf, f3 cf, float radiusf) {
-    double ox = (double)rOf.x - (double)cf.x, oy = (double)rOf.y - (double)cf.y, oz = (double)rOf.z - (double)cf.z;
-    const double r = (double)radiusf;
-    ox = ox / r;
-    oy = oy / r;
-    oz = oz / r;
-    const double dx = rDf.x, dy = rDf.y, dz = rDf.z;
-    double A = dx * dx + dy * dy + dz * dz;
-    double B = 2.0 * (dx * ox + dy * oy + dz * oz);
-    double C = (ox * ox + oy * oy + oz * oz) - 1.0;
-    double disc = B * B - 4.0 * A * C;
-    Isect is;
-    is.valid = false;
-    is.point = f3{0.0f, 0.0f, 0.0f};
-    is.t = 0.0f;
-    if (disc < 0.0) return is;
-    double t = (-B - sqrt(disc)) / (2.0 * A);
-    if (t < 0.0) t = (-B + sqrt(disc)) / (2.0 * A);
-    if (t >= 0.0) {
-        double px = (ox + t * dx) * r + (double)cf.x;
-        double py = (oy + t * dy) * r + (double)cf.y;
-        double pz = (oz + t * dz) * r + (double)cf.z;
-        is.valid = true;
-        is.point = f3{(float)px, (float)py, (float)pz};
-        double qx = px - ox, qy = py - oy, qz = pz - oz;
-        is.t = (float)sqrt(qx * qx + qy * qy + qz * qz);
-    }
-    return is;
-}
-
-// cloudRayMarch.comp:153-169
-MT_HD float remap(float v, float omin, float omax, float nmin, float nmax) {
-    return nmin + (((v - omin) / (omax - omin)) * (nmax - nmin));
-}
-MT_HD float remap_clamped(float v, float omin, float omax, float nmin, float nmax) {
-    float t = nmin + (((v - omin) / (omax - omin)) * (nmax - nmin));
-    return gclamp(t, nmin, nmax);
-}
-MT_HD float remap_clamped_ba(float v, float omin, float omax, float nmin, float nmax) {
-    v = gclamp(v, omin, omax);
-    float t = nmin + (((v - omin) / (omax - omin)) * (nmax - nmin));
-    return gclamp(t, nmin, nmax);
-}
-
-// cloudRayMarch.comp:171-186
-MT_HD float relative_height(const Frame& F, f3 point, f3 ec, f3 startPos, f3 rayDir, f3 eye) {
-    float lenCam = length3(point - eye);
-    float lenInner = length3(startPos - eye);
-    f3 p2e = normalize3_r(point - ec);
-    float cosTheta = dot3(rayDir, p2e);
-    float num = fabsf(cosTheta * (lenCam - lenInner));
-    return rdiv(num, F.r_thick);
-}
-
-// cloudRayMarch.comp:188-191
-MT_HD f3 relative_position(const Frame& F, f3 pos, f3 ec) {
-    const f3 d = pos - f3{ec.x, F.inner_alt, ec.z};
-    return f3{rdiv(d.x, F.r_thick), rdiv(d.y, F.r_thick), rdiv(d.z, F.r_thick)};
-}
-
-// cloudRayMarch.comp:475-487
-MT_HD float height_gradient(float h, float type) {
-    h = gclamp(h, 0.0f, 1.0f);
-    float stratocumulus = gmax(0.0f, remap_r(h, 0.0f, MT_RCP(0.0f, 0.25f), 0.0f, 1.0f) *
-                                         remap_r(h, 0.3f, MT_RCP(0.3f, 0.65f), 1.0f, 0.0f));
-    float stratus = gmax(0.0f, remap_r(h, 0.0f, MT_RCP(0.0f, 0.1f), 0.0f, 1.0f) *
-                                   remap_r(h, 0.2f, MT_RCP(0.2f, 0.3f), 1.0f, 0.0f));
-    float a = gmix(stratus, stratocumulus, gclamp(type * 2.0f, 0.0f, 1.0f));
-    float b = gmix(stratocumulus, stratus, gclamp((type - 0.5f) * 2.0f, 0.0f, 1.0f));
-    return gmix(a, b, type);
-}
-
-struct Weather {
-    float lo, mul, type;
-    float hgrad;  // height gradient at the primary sample, shared by its light samples
-    Rcp r_lo;     // 1 - lo, the coverage remap's width, shared by the step's samples
-};
-
-struct Tex {
-    const uint32_t* base;
-    const uint32_t* detail;
-    const uint32_t* curl;
-    const uint32_t* weather;
-};
-
-MT_HD Weather weather_at(const mt_params& p, const Frame& F, const Tex& tx, f3 pos, f3 ec) {
-    Weather w;
-    w.hgrad = 1.0f;
-    if (p.coverage_mode == 0) {
-        w.lo = p.coverage;
-        w.mul = p.coverage;
-        w.type = 0.0f;
-    } else {
-        f4v wd = tex2_u8<MT_WEATHER_N>(tx.weather, rdiv(pos.x - ec.x, F.r_weather), rdiv(pos.z - ec.z, F.r_weather));
-        w.lo = 1.0f - wd.x;
-        w.mul = wd.x;
-        w.type = wd.z;
-    }
-    w.r_lo = make_rcp(1.0f - w.lo);
-    return w;
-}
-
-// cloudRayMarch.comp:499-540
-MT_HD float sample_low_frequency(const mt_params& p, const Tex& tx, f3 point, float relH, const Weather& wt) {
-    f4v n = tex3_u8<MT_BASE_N>(tx.base, point);
-    float fbm = (n.y * 0.625f) + (n.z * 0.25f) + (n.w * 0.125f);
-    fbm = gclamp(fbm, 0.0f, 1.0f);
-    float baseCloud = remap_clamped(n.x, (fbm - 0.9f), 1.0f, 0.0f, 1.0f);
-    // getDensityHeightGradientForPoint(relH, type): every call of a step passes
-    // the primary sample's height and weather, so it is evaluated once per step
-    // (Weather::hgrad).
-    if (p.height_gradient) baseCloud = baseCloud * wt.hgrad;
-    // remapClampedBeforeAndAfter(baseCloud, lo, 1, 0, 1) with its width 1 - lo
-    // shared by the step's samples
-    float v = gclamp(baseCloud, wt.lo, 1.0f);
-    float bc = gclamp(0.0f + ((rdiv(v - wt.lo, wt.r_lo)) * (1.0f - 0.0f)), 0.0f, 1.0f);
-    return bc * wt.mul;
-}
-
-// cloudRayMarch.comp:542-563.  The texture part is the same for the primary
-// erosion (:645) and the six cone-light erosions (:665): all are evaluated at
-// the primary sample point with the primary height, so it is computed once.
-MT_HD float erosion_modifier(const Tex& tx, f3 point, float h) {
-    f4v curl = tex2_u8<MT_CURL_N>(tx.curl, point.x, point.y);
-    point.x = point.x + (curl.x * (1.0f - h)) * 0.5f;
-    point.y = point.y + (curl.y * (1.0f - h)) * 0.5f;
-    f4v hf = tex3_u8<MT_DETAIL_N>(tx.detail, point);
-    float hfbm = (hf.x * 0.625f) + (hf.y * 0.25f) + (hf.z * 0.125f);
-    return gclamp(gmix(hfbm, 1.0f - hfbm, gclamp(h * 2.0f, 0.0f, 1.0f)), 0.0f, 1.0f);
-}
-struct Erosion {
-    float lo;  // high_freq_modifier * 0.005
-    Rcp r;     // 1 - lo, shared by the step's seven erosions
-};
-MT_HD Erosion make_erosion(float modifier) {
-    Erosion e;
-    e.lo = modifier * 0.005f;
-    e.r = make_rcp(1.0f - e.lo);
-    return e;
-}
-MT_HD float erode(float baseCloud, const Erosion& e) { return remap_r(baseCloud, e.lo, e.r, 0.0f, 1.0f); }
-
-// cloudRayMarch.comp:295-306
-MT_HD float henyey_greenstein(float c, float e) {
-    float num = 1.0f - e * e;
-    float den = powf((1.0f + e * e - 2.0f * e * c), 1.5f);
-    return (num / den) * 0.07957747154594767f;
-}
-
-// cloudRayMarch.comp:331-388.  cos_q = (cos_angle - 0.7) / (1.0 - 0.7), the
-// ray-constant quotient of the attenuation remap (:341-343).
-MT_HD float light_energy(float h, float dl, float ds, float phase, float cos_q, float brightness) {
-    const float primary = expf(-dl);
-    const float secondary = primary;  // exp(-dl) twice in the reference (:334, :340)
-    float att = gmax(secondary + (cos_q * (secondary * 0.25f - secondary)), primary);
-    float depth = 0.05f + pow_nl(ds, gclamp(remap_r(h * 0.125f, 0.3f, MT_RCP(0.3f, 0.85f), 0.5f, 2.0f), 0.5f, 2.0f));
-    float vert = pow_nl(gclamp(remap_r(h * 1.5f, 0.07f, MT_RCP(0.07f, 0.34f), 0.1f, 1.0f), 0.1f, 1.0f), 0.8f);
-    float in_scatter = depth * vert;
-    return att * primary * in_scatter * phase * brightness;
-}
-
-// cloudRayMarch.comp:401-467 (Preetham).  Once per ray: kept out of line so
-// the march loop stays small in the instruction cache.
-__device__ __noinline__ f3 atmosphere_color(const mt_params& p, f3 dir, f3 sunDir, float sunIntensity) {
-    const f3 skySun = ld3(p.sky_sun_pos);
-    const float PI = 3.14159265f;
-    sunDir = normalize3(sunDir);
-    float zenithAngleCos = gclamp(normalize3(skySun).y, -1.0f, 1.0f);
-    float sunI = 1000.0f * gmax(0.0f, 1.0f - powf(2.718281828459f, -((1.6110731557f - acosf(zenithAngleCos)) / 1.5f)));
-    float sunE = sunIntensity * sunI;
-    float sunFade = 1.0f - gclamp(1.0f - expf(skySun.y / 450000.0f), 0.0f, 1.0f);
-    const f3 RT{5.804542996261093E-6f, 1.3562911419845635E-5f, 3.0265902468824876E-5f};
-    f3 BetaR = RT * (2.0f - 1.0f + sunFade);
-    float c = (0.2f * 10.0f) * 10E-18f;
-    const f3 MIE{1.839991851443397f, 2.779802391966052f, 4.079047954386109f};
-    f3 BetaM = ((0.434f * c) * MIE) * 0.005f;
-    float zenith = acosf(gmax(0.0f, dir.y));
-    float inverse = 1.0f / (cosf(zenith) + 0.15f * powf(93.885f - ((zenith * 180.0f) / PI), -1.253f));
-    float sR = 8.4E3f * inverse;
-    float sM = 1.25E3f * inverse;
-    f3 ex = (-BetaR) * sR + BetaM * sM;
-    f3 fex{expf(ex.x), expf(ex.y), expf(ex.z)};
-    float cosTheta = dot3(sunDir, dir);
-    float rp = cosTheta * 0.5f + 0.5f;
-    float rPhase = 0.05968310365946075f * (1.0f + rp * rp);
-    f3 betaRTheta = BetaR * rPhase;
-    float mPhase = henyey_greenstein(cosTheta, 0.8f);
-    f3 betaMTheta = BetaM * mPhase;
-    float yDot = 1.0f - sunDir.y;
-    yDot = yDot * (yDot * yDot * yDot * yDot);
-    f3 betas = (betaRTheta + betaMTheta) / (BetaR + BetaM);
-    f3 a = (sunE * betas) * (f3{1.0f, 1.0f, 1.0f} - fex);
-    f3 Lin{powf(a.x, 1.5f), powf(a.y, 1.5f), powf(a.z, 1.5f)};
-    f3 b = (sunE * betas) * fex;
-    f3 pb{powf(b.x, 0.5f), powf(b.y, 0.5f), powf(b.z, 0.5f)};
-    Lin = Lin * mix3(f3{1.0f, 1.0f, 1.0f}, pb, gclamp(yDot, 0.0f, 1.0f));
-    f3 L0 = 0.1f * fex;
-    const float SAC = 0.999956676946448443553574619906976478926848692873900859324f;
-    float sunDisk = gsmoothstep(SAC, SAC + 0.00002f, cosTheta);
-    L0 = L0 + ((sunE * 15000.0f) * fex) * sunDisk;
-    return (Lin + L0) * 0.04f + f3{0.0f, 0.0003f, 0.00075f};
-}
-
-struct Counts {
-    unsigned primary, light, rays;
-};
-
-// Per-ray constants of cloudRayMarch.comp:565-624, shared by every step.
-struct RayConsts {
-    Ray ray;
-    f3 ec, startPos;
-    f3 kernel[6];
-    f3 wind, skew;
-    float stepSize, cos_angle, cos_q, HG_light, total_time;
-    int pixelID;
-};
-
-__device__ __noinline__ void ray_consts(const mt_params& p, const mt_time_ubo& tm, const Ray& ray, f3 ec,
-                                        f3 startPos, float stepSize, int pixelID, RayConsts& rc) {
-    rc.ray = ray;
-    rc.ec = ec;
-    rc.startPos = startPos;
-    rc.stepSize = stepSize;
-    rc.pixelID = pixelID;
-    const f3 lightDir = normalize3(ld3(p.sun_light_pos) - ray.origin);
-    rc.cos_angle = dot3(normalize3(ray.direction), lightDir);
-    rc.cos_q = (rc.cos_angle - 0.7f) / (1.0f - 0.7f);
-    rc.HG_light = gmax(henyey_greenstein(rc.cos_angle, 0.6f), 0.7f * henyey_greenstein(rc.cos_angle, 0.99f - 0.1f));
-    float ax = fabsf(lightDir.x), ay = fabsf(lightDir.y), az = fabsf(lightDir.z);
-    f3 maxComp;
-    if (ax > ay && ax > az)
-        maxComp = f3{ax, 0.0f, 0.0f};
-    else if (ay > ax && ay > az)
-        maxComp = f3{0.0f, ay, 0.0f};
-    else
-        maxComp = f3{0.0f, 0.0f, az};
-    f3 zC = cross3(lightDir, maxComp);
-    f3 xC = cross3(zC, lightDir);
-    rc.kernel[0] = mat3mul(xC, lightDir, zC, f3{0.1f, 0.25f, -0.15f});
-    rc.kernel[1] = mat3mul(xC, lightDir, zC, f3{0.2f, 0.5f, 0.2f});
-    rc.kernel[2] = mat3mul(xC, lightDir, zC, f3{-0.2f, 0.1f, -0.1f});
-    rc.kernel[3] = mat3mul(xC, lightDir, zC, f3{-0.05f, 0.75f, 0.05f});
-    rc.kernel[4] = mat3mul(xC, lightDir, zC, f3{-0.1f, 1.0f, 0.0f});
-    rc.kernel[5] = mat3mul(xC, lightDir, zC, f3{0.0f, 3.0f, 0.0f});
-    rc.wind = ld3(p.wind_dir) * p.wind_speed;
-    rc.skew = ld3(p.skew_dir);
-    rc.total_time = tm.time[1];
-}
-
-struct StepOut {
-    int in_cloud;  // baseDensity > 0 (cloudRayMarch.comp:642)
-    float hfd;     // eroded density (:645)
-    float E;       // light energy (:673)
-};
-
-// One iteration of the march loop body (cloudRayMarch.comp:629-678) at
-// parameter t, up to the accumulation: everything that does not depend on the
-// running accumDensity / transmittance.
-MT_HD StepOut eval_step(const mt_params& p, const Frame& F, const Tex& tx, const mt_time_ubo& tm,
-                        const RayConsts& rc, float t) {
-    StepOut o{0, 0.0f, 0.0f};
-    int _index = f2i(gmod((float)(rc.pixelID + f2i(t)), 16.0f));
-    float jx, jy;
-    jitter_offset(tm, _index, 1.0f, 1.0f, false, jx, jy);  // halton values; / 75 below
-    jx = rdiv(jx, MT_RCP(0.0f, 75.0f));
-    jy = rdiv(jy, MT_RCP(0.0f, 75.0f));
-    f3 jd = rc.ray.direction + f3{jx, (jx + jy) * 1.180f, jy};
-    f3 pos = rc.ray.origin + t * jd;
-    f3 sp = relative_position(F, pos, rc.ec);
-    sp = f3{rdiv(sp.x, F.r_period), rdiv(sp.y, F.r_period), rdiv(sp.z, F.r_period)};
-    float relH = relative_height(F, pos, rc.ec, rc.startPos, rc.ray.direction, rc.ray.origin);
-    sp = sp + ((relH * rc.skew) * p.cloud_top_offset) * 0.009f;
-    sp = sp + rc.wind * rc.total_time;
-    Weather wt = weather_at(p, F, tx, pos, rc.ec);
-    if (p.height_gradient) wt.hgrad = height_gradient(relH, wt.type);
-    float baseDensity = sample_low_frequency(p, tx, sp, relH, wt) * 0.380f;
-    if (baseDensity > 0.0f) {
-        const Erosion ero = make_erosion(erosion_modifier(tx, sp, relH));
-        o.in_cloud = 1;
-        o.hfd = erode(baseDensity * 1.4f, ero);
-        float dl = 0.0f;
-        // Kept rolled: six inlined copies of the sampler overflow the
-        // instruction cache (the dominant stall when unrolled).
-#pragma unroll 1
-        for (int i = 0; i < 6; ++i) {
-            f3 lightPos = pos + ((rc.stepSize * rc.kernel[i]) * (float)i);
-            f3 slp = relative_position(F, lightPos, rc.ec);
-            float cbl = sample_low_frequency(p, tx, slp, relH, wt);
-            if (cbl > 0.0f) dl = dl + erode(1.5f * cbl, ero);
-        }
-        o.E = light_energy(relH, dl, baseDensity, rc.HG_light, rc.cos_q, 5.0f);
-    }
-    return o;
-}
-
-// cloudRayMarch.comp:565-688, step-parallel.  A group of G lanes marches one
-// ray: lane j evaluates step c*G + j of chunk c, with t rebuilt by the same
-// serial `t += stepSize` additions as the reference's loop, so every lane sees
-// bit-identical t.  The loop-carried part (accumDensity, transmittance,
-// colour, the early exit) is then applied in step order by an in-group scan;
-// steps past the exit are discarded.  Result, counters and control flow equal
-// the sequential loop's.
-template <int G>
-MT_HD f3 ray_march_group(const mt_params& p, const Frame& F, const Tex& tx, const mt_time_ubo& tm, const Ray& ray,
-                         f3 ec, f3 startPos, float start_t, float end_t, int pixelID, float& accum, Counts& cnt,
-                         unsigned gmask, int lane) {
-    float _dot = dot3(ray.direction, f3{0.0f, 1.0f, 0.0f});
-    float maxSteps;
-    if (p.steps_min == p.steps_max)
-        maxSteps = (float)p.steps_min;
-    else
-        maxSteps = floorf(gmix((float)p.steps_min, (float)p.steps_max, 1.0f - _dot));
-    const float thick = end_t - start_t;
-    const float stepSize = thick / maxSteps;
-    RayConsts rc;
-    ray_consts(p, tm, ray, ec, startPos, stepSize, pixelID, rc);
-    float transmittance = 1.0f;
-    f3 color{0.0f, 0.0f, 0.0f};
-    // Iteration guard (not in the reference): a step below the ulp of t would
-    // never advance.  A valid ray runs steps or steps+1 iterations.
-    const int cap = 2 * f2i(maxSteps) + 8;
-    if (lane == 0) cnt.rays++;
-    float t_base = start_t;
-    int s_base = 0;
-    bool done = false;
-    while (!done) {
-        float t = t_base;
-        for (int k = 0; k < lane; ++k) t += stepSize;
-        const int valid = (t < end_t) && (s_base + lane < cap);
-        StepOut o{0, 0.0f, 0.0f};
-        if (valid) o = eval_step(p, F, tx, tm, rc, t);
-#pragma unroll
-        for (int k = 0; k < G; ++k) {
-            if (!__shfl_sync(gmask, valid, k, G)) {
-                done = true;
-                break;
-            }
-            const int in_cloud = __shfl_sync(gmask, o.in_cloud, k, G);
-            const float hfd = __shfl_sync(gmask, o.hfd, k, G);
-            const float E = __shfl_sync(gmask, o.E, k, G);
-            if (lane == 0) cnt.primary++;
-            if (in_cloud) {
-                accum = accum + hfd * 0.5f;
-                transmittance = gmix(transmittance, E, (1.0f - accum));
-                color = color + f3{transmittance, transmittance, transmittance};
-                if (lane == 0) cnt.light += 6;
-            }
-            if (accum >= p.accum_limit) {
-                accum = 1.0f;
-                done = true;
-                break;
-            }
-        }
-        if (!done) {
-            t_base = __shfl_sync(gmask, t, G - 1, G) + stepSize;
-            s_base += G;
-        }
-    }
-    return color;
-}
-
-// cloudRayMarch.comp:106-112 + postProcess_GodRays.frag:36-43
-MT_HD float godray_value(float v, float dir_y) {
-    f4v enc{1.0f * v, 255.0f * v, 65025.0f * v, 16581375.0f * v};
-    enc = f4v{gfract(enc.x), gfract(enc.y), gfract(enc.z), gfract(enc.w)};
-    const float k = 1.0f / 255.0f;
-    enc = f4v{enc.x - enc.y * k, enc.y - enc.z * k, enc.z - enc.w * k, enc.w - enc.w * 0.0f};
-    if (dir_y < 0.05f) enc = enc * gmax(5.0f, dir_y);
-    return enc.x * (1.0f / 1.0f) + enc.y * (1.0f / 255.0f) + enc.z * (1.0f / 65025.0f) + enc.w * (1.0f / 16581375.0f);
-}
-
-// cloudRayMarch.comp:690-826 for one pixel, marched by a group of G lanes;
-// lane 0 stores.
-template <int G>
-MT_HD void march_pixel(const MarchArgs& a, const Frame& F, const Tex& tx, int px, int py, Counts& cnt,
-                       unsigned gmask, int lane) {
-    const mt_params& p = a.params;
-    const int W = a.width, H = a.height;
-    const int pixelID = a.time.frame_count_mod16;
-    float ux = (float)px / (float)W, uy = (float)py / (float)H;
-    uy = 1.0f - uy;
-    f3 eyePos = p.eye_sign * ld3(a.camera.eye);
-    Ray ray = cast_ray(ux, uy, eyePos, a.camera, a.time, pixelID, W, H, false);
-    const float sunIntensity = 0.780f;
-    float _dot = dot3(f3{0.0f, 1.0f, 0.0f}, ray.direction);
-    const float bgMul = gmax(0.620f, _dot);
-    const float fade = 0.06f;
-    const size_t o = (size_t)py * (size_t)W + (size_t)px;
-    f3 bg;
-    if (_dot < 0.0f) {
-        f3 cNear = f3{0.0f, 0.16f, 0.51f} * 0.4f;
-        f3 c2 = f3{0.0f, 0.73f, 0.95f} * 0.5f;
-        bg = mix3(cNear, c2, -ray.direction.y * 5.5f);
-        if (lane == 0) {
-            a.cur[o] = make_float4(bg.x, bg.y, bg.z, 1.0f);
-            if (a.mask) a.mask[o] = 0.0f;
-        }
-        return;
-    }
-    bg = atmosphere_color(p, ray.direction, ld3(p.sky_sun_pos) - ray.origin, sunIntensity);
-    bg = bg * bgMul;
-    if (_dot < fade) {
-        if (lane == 0) {
-            a.cur[o] = make_float4(bg.x, bg.y, bg.z, 1.0f);
-            if (a.mask) a.mask[o] = 0.0f;
-        }
-        return;
-    }
-    f3 ec = eyePos;
-    ec.y = -F.R;
-    Isect in, out;
-    if (p.fp64_shells) {
-        in = ray_sphere_fp64(ray.origin, ray.direction, ec, F.Rin);
-        out = ray_sphere_fp64(ray.origin, ray.direction, ec, F.Rout);
-    } else {
-        in = ray_sphere(ray.origin, ray.direction, ec, F.Rin);
-        out = ray_sphere(ray.origin, ray.direction, ec, F.Rout);
-    }
-    float accum = 0.0f;
-    f3 res = ray_march_group<G>(p, F, tx, a.time, ray, ec, in.point, in.t, out.t, pixelID, accum, cnt, gmask, lane);
-    if (lane != 0) return;
-    float godAccum = accum;
-    accum = accum * gsmoothstep(0.0f, 1.0f, gmin(1.0f, remap(ray.direction.y, fade, 0.2f, 0.0f, 1.0f)));
-    f3 fc = mix3(bg, res, accum);
-    a.cur[o] = make_float4(fc.x, fc.y, fc.z, 1.0f);
-    if (a.mask) a.mask[o] = godray_value(25.0f * gmin(0.05f, 1.0f - godAccum), ray.direction.y);
-}
-
-__device__ __forceinline__ void flush_counts(unsigned long long* stats, const Counts& c, unsigned pixels) {
-    unsigned prim = __reduce_add_sync(0xffffffffu, c.primary);
-    unsigned light = __reduce_add_sync(0xffffffffu, c.light);
-    unsigned rays = __reduce_add_sync(0xffffffffu, c.rays);
-    unsigned pix = __reduce_add_sync(0xffffffffu, pixels);
-    if ((threadIdx.x & 31) == 0) {
-        atomicAdd(stats + 0, (unsigned long long)prim);
-        atomicAdd(stats + 1, (unsigned long long)light);
-        atomicAdd(stats + 2, (unsigned long long)rays);
-        atomicAdd(stats + 3, (unsigned long long)pix);
-    }
-}
-
-// Ray -> marched pixel.  Checkerboard: the reference's group grid covers
-// groups_x x groups_y blocks of 4x4 (Renderer.cpp:713-716); each ray is one
-// block's slot pixel.  Full: one ray per pixel.  G consecutive lanes (an
-// aligned segment of a warp) march one ray.
-template <int G>
-__global__ void __launch_bounds__(128, 8) march_kernel(const __grid_constant__ MarchArgs a) {
-    static_assert(G >= 1 && G <= 32 && (32 % G) == 0, "G must divide the warp");
-    const Frame F = make_frame(a.params);
-    const Tex tx{a.base, a.detail, a.curl, a.weather};
-    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long idx = tid / G;
-    const int lane = (int)(threadIdx.x % G);
-    const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
-    Counts cnt{0u, 0u, 0u};
-    unsigned pixels = 0;
-    int px = 0, py = 0;
-    bool active;
-    if (a.flags & MT_RENDER_FULL) {
-        active = idx < (long long)a.width * a.height;
-        if (active) {
-            px = (int)(idx % a.width);
-            py = (int)(idx / a.width);
-        }
-    } else {
-        active = idx < (long long)a.groups_x * a.groups_y;
-        if (active) {
-            const int id = a.time.frame_count_mod16;
-            px = (int)(idx % a.groups_x) * 4 + a.params.slot_x[id];
-            py = (int)(idx / a.groups_x) * 4 + a.params.slot_y[id];
-            active = px < a.width && py < a.height;
-        }
-    }
-    if (active) {
-        march_pixel<G>(a, F, tx, px, py, cnt, gmask, lane);
-        pixels = lane == 0 ? 1u : 0u;
-    }
-    if (a.stats) flush_counts(a.stats, cnt, pixels);
-}
 
 // Pixels the checkerboard raymarch writes this frame (cloudRayMarch.comp:695-701
 // under the dispatch of Renderer.cpp:713-716).
@@ -823,18 +237,16 @@ static cudaError_t launch_march(const MarchArgs& a, cudaStream_t s, const Launch
     // Images narrower or shorter than 4 pixels give the reference an empty
     // raymarch dispatch (Renderer.cpp:713-716): nothing is marched.
     if (timed) cudaEventRecord(ev->march[0], s);
+    cudaError_t e = cudaSuccess;
     if (m > 0) {
-        const int G = a.lanes;
-        const unsigned blocks = (unsigned)((m * G + 127) / 128);
-        switch (G) {
-            case 1: march_kernel<1><<<blocks, 128, 0, s>>>(a); break;
-            case 4: march_kernel<4><<<blocks, 128, 0, s>>>(a); break;
-            case 16: march_kernel<16><<<blocks, 128, 0, s>>>(a); break;
-            default: march_kernel<8><<<blocks, 128, 0, s>>>(a); break;
+        switch (a.params.storage) {
+            case MT_STORAGE_F16: e = launch_march_f16(a, s, m); break;
+            case MT_STORAGE_BF16: e = launch_march_bf16(a, s, m); break;
+            default: e = launch_march_u8(a, s, m); break;
         }
     }
     if (timed) cudaEventRecord(ev->march[1], s);
-    return cudaGetLastError();
+    return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 cudaError_t launch_render(const MarchArgs& a, cudaStream_t s, const LaunchEvents* ev) {

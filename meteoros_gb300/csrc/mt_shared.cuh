@@ -1,0 +1,290 @@
+// Geometry, lighting and sky functions of the compute stage shared by every
+// kernel translation unit (FP32, reference operation order; see
+// mt_device.cuh for the arithmetic conventions).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "mt_device.cuh"
+#include "mt_kernels.h"
+
+namespace mt {
+
+struct Frame {
+    float R, Rin, Rout, thickness, inner_alt;
+    Rcp r_thick, r_period, r_weather;  // per-frame denominators (see rdiv)
+};
+
+MT_HD Frame make_frame(const mt_params& p) {
+    Frame F;
+    F.R = p.earth_radius;
+    F.Rin = p.shell_inner_radius;
+    F.Rout = p.shell_outer_radius;
+    F.thickness = F.Rout - F.Rin;
+    F.inner_alt = F.Rin - F.R;
+    F.r_thick = make_rcp(F.thickness);
+    F.r_period = make_rcp(p.noise_period);
+    F.r_weather = make_rcp(p.weather_scale);
+    return F;
+}
+
+// remap() whose range width omax - omin is known ahead: the quotient through
+// the correctly rounded reciprocal of that width (rdiv).
+MT_HD float remap_r(float v, float omin, Rcp width, float nmin, float nmax) {
+    return nmin + ((rdiv(v - omin, width)) * (nmax - nmin));
+}
+// The reciprocal of a compile-time width, rounded once by the compiler.
+#define MT_RCP(omin, omax) (Rcp{(omax) - (omin), 1.0f / ((omax) - (omin))})
+
+struct Ray {
+    f3 origin, direction;
+};
+struct Isect {
+    f3 point;
+    bool valid;
+    float t;
+};
+
+// cloudRayMarch.comp:114-132; reprojection.comp:72-90 reads halton 1/2 again
+// for index >= 4 (`repro`).
+MT_HD void jitter_offset(const mt_time_ubo& tm, int index, float dimx, float dimy, bool repro, float& jx,
+                         float& jy) {
+    index = index / 2;
+    float x, y;
+    if (index < 4) {
+        x = tm.halton_seq1[index];
+        y = tm.halton_seq2[index];
+    } else {
+        index -= 4;
+        if (repro) {
+            x = tm.halton_seq1[index];
+            y = tm.halton_seq2[index];
+        } else {
+            x = tm.halton_seq3[index];
+            y = tm.halton_seq4[index];
+        }
+    }
+    jx = x / dimx;
+    jy = y / dimy;
+}
+
+// cloudRayMarch.comp:194-226
+MT_HD Ray cast_ray(float sx, float sy, f3 eye, const mt_camera_ubo& cam, const mt_time_ubo& tm, int pixelID, int W,
+                   int H, bool repro) {
+    const float* v = cam.view;
+    f3 camRight = normalize3(f3{v[0], v[4], v[8]});
+    f3 camUp = normalize3(f3{v[1], v[5], v[9]});
+    f3 camLook = -normalize3(f3{v[2], v[6], v[10]});
+    float nx = sx * 2.0f - 1.0f, ny = sy * 2.0f - 1.0f;
+    float jx, jy;
+    jitter_offset(tm, pixelID, (float)W, (float)H, repro, jx, jy);
+    nx = nx + jx;
+    ny = ny + jy;
+    f3 cam_x = (nx * cam.tan_fov_by_2[0]) * camRight;
+    f3 cam_y = (ny * cam.tan_fov_by_2[1]) * camUp;
+    f3 ref = eye + camLook;
+    f3 pp = ref + cam_x + cam_y;
+    return Ray{eye, normalize3(pp - eye)};
+}
+
+// cloudRayMarch.comp:229-273 (t = length(p - rO) with the normalised rO, as
+// the reference defines it).
+MT_HD Isect ray_sphere(f3 rO, f3 rD, f3 c, float radius) {
+    Isect is;
+    is.valid = false;
+    is.point = f3{0.0f, 0.0f, 0.0f};
+    is.t = 0.0f;
+    rO = rO - c;
+    rO = rO / radius;
+    float A = dot3(rD, rD);
+    float B = 2.0f * dot3(rD, rO);
+    float C = dot3(rO, rO) - 1.0f;
+    float disc = B * B - 4.0f * A * C;
+    if (disc < 0.0f) return is;
+    float t = (-B - sqrtf(disc)) / (2.0f * A);
+    if (t < 0.0f) t = (-B + sqrtf(disc)) / (2.0f * A);
+    if (t >= 0.0f) {
+        f3 pnt = rO + t * rD;
+        is.valid = true;
+        pnt = pnt * radius;
+        pnt = pnt + c;
+        is.point = pnt;
+        is.t = length3(pnt - rO);
+    }
+    return is;
+}
+
+// The same intersection in FP64 (precision form): the normalised-sphere
+// quadratic cancels badly in FP32 (C = |rO|^2 - 1 with |rO| ~ 1).
+MT_HD Isect ray_sphere_fp64(f3 rOf, f3 rDf, f3 cf, float radiusf) {
+    double ox = (double)rOf.x - (double)cf.x, oy = (double)rOf.y - (double)cf.y, oz = (double)rOf.z - (double)cf.z;
+    const double r = (double)radiusf;
+    ox = ox / r;
+    oy = oy / r;
+    oz = oz / r;
+    const double dx = rDf.x, dy = rDf.y, dz = rDf.z;
+    double A = dx * dx + dy * dy + dz * dz;
+    double B = 2.0 * (dx * ox + dy * oy + dz * oz);
+    double C = (ox * ox + oy * oy + oz * oz) - 1.0;
+    double disc = B * B - 4.0 * A * C;
+    Isect is;
+    is.valid = false;
+    is.point = f3{0.0f, 0.0f, 0.0f};
+    is.t = 0.0f;
+    if (disc < 0.0) return is;
+    double t = (-B - sqrt(disc)) / (2.0 * A);
+    if (t < 0.0) t = (-B + sqrt(disc)) / (2.0 * A);
+    if (t >= 0.0) {
+        double px = (ox + t * dx) * r + (double)cf.x;
+        double py = (oy + t * dy) * r + (double)cf.y;
+        double pz = (oz + t * dz) * r + (double)cf.z;
+        is.valid = true;
+        is.point = f3{(float)px, (float)py, (float)pz};
+        double qx = px - ox, qy = py - oy, qz = pz - oz;
+        is.t = (float)sqrt(qx * qx + qy * qy + qz * qz);
+    }
+    return is;
+}
+
+// cloudRayMarch.comp:153-169
+MT_HD float remap(float v, float omin, float omax, float nmin, float nmax) {
+    return nmin + (((v - omin) / (omax - omin)) * (nmax - nmin));
+}
+MT_HD float remap_clamped(float v, float omin, float omax, float nmin, float nmax) {
+    float t = nmin + (((v - omin) / (omax - omin)) * (nmax - nmin));
+    return gclamp(t, nmin, nmax);
+}
+MT_HD float remap_clamped_ba(float v, float omin, float omax, float nmin, float nmax) {
+    v = gclamp(v, omin, omax);
+    float t = nmin + (((v - omin) / (omax - omin)) * (nmax - nmin));
+    return gclamp(t, nmin, nmax);
+}
+
+// cloudRayMarch.comp:171-186
+MT_HD float relative_height(const Frame& F, f3 point, f3 ec, f3 startPos, f3 rayDir, f3 eye) {
+    float lenCam = length3(point - eye);
+    float lenInner = length3(startPos - eye);
+    f3 p2e = normalize3_r(point - ec);
+    float cosTheta = dot3(rayDir, p2e);
+    float num = fabsf(cosTheta * (lenCam - lenInner));
+    return rdiv(num, F.r_thick);
+}
+
+// cloudRayMarch.comp:188-191
+MT_HD f3 relative_position(const Frame& F, f3 pos, f3 ec) {
+    const f3 d = pos - f3{ec.x, F.inner_alt, ec.z};
+    return f3{rdiv(d.x, F.r_thick), rdiv(d.y, F.r_thick), rdiv(d.z, F.r_thick)};
+}
+
+// cloudRayMarch.comp:475-487
+MT_HD float height_gradient(float h, float type) {
+    h = gclamp(h, 0.0f, 1.0f);
+    float stratocumulus = gmax(0.0f, remap_r(h, 0.0f, MT_RCP(0.0f, 0.25f), 0.0f, 1.0f) *
+                                         remap_r(h, 0.3f, MT_RCP(0.3f, 0.65f), 1.0f, 0.0f));
+    float stratus = gmax(0.0f, remap_r(h, 0.0f, MT_RCP(0.0f, 0.1f), 0.0f, 1.0f) *
+                                   remap_r(h, 0.2f, MT_RCP(0.2f, 0.3f), 1.0f, 0.0f));
+    float a = gmix(stratus, stratocumulus, gclamp(type * 2.0f, 0.0f, 1.0f));
+    float b = gmix(stratocumulus, stratus, gclamp((type - 0.5f) * 2.0f, 0.0f, 1.0f));
+    return gmix(a, b, type);
+}
+
+struct Erosion {
+    float lo;  // high_freq_modifier * 0.005
+    Rcp r;     // 1 - lo, shared by the step's seven erosions
+};
+MT_HD Erosion make_erosion(float modifier) {
+    Erosion e;
+    e.lo = modifier * 0.005f;
+    e.r = make_rcp(1.0f - e.lo);
+    return e;
+}
+MT_HD float erode(float baseCloud, const Erosion& e) { return remap_r(baseCloud, e.lo, e.r, 0.0f, 1.0f); }
+
+// cloudRayMarch.comp:295-306
+MT_HD float henyey_greenstein(float c, float e) {
+    float num = 1.0f - e * e;
+    float den = powf((1.0f + e * e - 2.0f * e * c), 1.5f);
+    return (num / den) * 0.07957747154594767f;
+}
+
+// cloudRayMarch.comp:331-388.  cos_q = (cos_angle - 0.7) / (1.0 - 0.7), the
+// ray-constant quotient of the attenuation remap (:341-343).
+MT_HD float light_energy(float h, float dl, float ds, float phase, float cos_q, float brightness) {
+    const float primary = expf(-dl);
+    const float secondary = primary;  // exp(-dl) twice in the reference (:334, :340)
+    float att = gmax(secondary + (cos_q * (secondary * 0.25f - secondary)), primary);
+    float depth = 0.05f + pow_nl(ds, gclamp(remap_r(h * 0.125f, 0.3f, MT_RCP(0.3f, 0.85f), 0.5f, 2.0f), 0.5f, 2.0f));
+    float vert = pow_nl(gclamp(remap_r(h * 1.5f, 0.07f, MT_RCP(0.07f, 0.34f), 0.1f, 1.0f), 0.1f, 1.0f), 0.8f);
+    float in_scatter = depth * vert;
+    return att * primary * in_scatter * phase * brightness;
+}
+
+// cloudRayMarch.comp:401-467 (Preetham).  Once per ray: kept out of line so
+// the march loop stays small in the instruction cache.
+static __device__ __noinline__ f3 atmosphere_color(const mt_params& p, f3 dir, f3 sunDir, float sunIntensity) {
+    const f3 skySun = ld3(p.sky_sun_pos);
+    const float PI = 3.14159265f;
+    sunDir = normalize3(sunDir);
+    float zenithAngleCos = gclamp(normalize3(skySun).y, -1.0f, 1.0f);
+    float sunI = 1000.0f * gmax(0.0f, 1.0f - powf(2.718281828459f, -((1.6110731557f - acosf(zenithAngleCos)) / 1.5f)));
+    float sunE = sunIntensity * sunI;
+    float sunFade = 1.0f - gclamp(1.0f - expf(skySun.y / 450000.0f), 0.0f, 1.0f);
+    const f3 RT{5.804542996261093E-6f, 1.3562911419845635E-5f, 3.0265902468824876E-5f};
+    f3 BetaR = RT * (2.0f - 1.0f + sunFade);
+    float c = (0.2f * 10.0f) * 10E-18f;
+    const f3 MIE{1.839991851443397f, 2.779802391966052f, 4.079047954386109f};
+    f3 BetaM = ((0.434f * c) * MIE) * 0.005f;
+    float zenith = acosf(gmax(0.0f, dir.y));
+    float inverse = 1.0f / (cosf(zenith) + 0.15f * powf(93.885f - ((zenith * 180.0f) / PI), -1.253f));
+    float sR = 8.4E3f * inverse;
+    float sM = 1.25E3f * inverse;
+    f3 ex = (-BetaR) * sR + BetaM * sM;
+    f3 fex{expf(ex.x), expf(ex.y), expf(ex.z)};
+    float cosTheta = dot3(sunDir, dir);
+    float rp = cosTheta * 0.5f + 0.5f;
+    float rPhase = 0.05968310365946075f * (1.0f + rp * rp);
+    f3 betaRTheta = BetaR * rPhase;
+    float mPhase = henyey_greenstein(cosTheta, 0.8f);
+    f3 betaMTheta = BetaM * mPhase;
+    float yDot = 1.0f - sunDir.y;
+    yDot = yDot * (yDot * yDot * yDot * yDot);
+    f3 betas = (betaRTheta + betaMTheta) / (BetaR + BetaM);
+    f3 a = (sunE * betas) * (f3{1.0f, 1.0f, 1.0f} - fex);
+    f3 Lin{powf(a.x, 1.5f), powf(a.y, 1.5f), powf(a.z, 1.5f)};
+    f3 b = (sunE * betas) * fex;
+    f3 pb{powf(b.x, 0.5f), powf(b.y, 0.5f), powf(b.z, 0.5f)};
+    Lin = Lin * mix3(f3{1.0f, 1.0f, 1.0f}, pb, gclamp(yDot, 0.0f, 1.0f));
+    f3 L0 = 0.1f * fex;
+    const float SAC = 0.999956676946448443553574619906976478926848692873900859324f;
+    float sunDisk = gsmoothstep(SAC, SAC + 0.00002f, cosTheta);
+    L0 = L0 + ((sunE * 15000.0f) * fex) * sunDisk;
+    return (Lin + L0) * 0.04f + f3{0.0f, 0.0003f, 0.00075f};
+}
+
+struct Counts {
+    unsigned primary, light, rays;
+};
+
+// cloudRayMarch.comp:106-112 + postProcess_GodRays.frag:36-43
+MT_HD float godray_value(float v, float dir_y) {
+    f4v enc{1.0f * v, 255.0f * v, 65025.0f * v, 16581375.0f * v};
+    enc = f4v{gfract(enc.x), gfract(enc.y), gfract(enc.z), gfract(enc.w)};
+    const float k = 1.0f / 255.0f;
+    enc = f4v{enc.x - enc.y * k, enc.y - enc.z * k, enc.z - enc.w * k, enc.w - enc.w * 0.0f};
+    if (dir_y < 0.05f) enc = enc * gmax(5.0f, dir_y);
+    return enc.x * (1.0f / 1.0f) + enc.y * (1.0f / 255.0f) + enc.z * (1.0f / 65025.0f) + enc.w * (1.0f / 16581375.0f);
+}
+
+__device__ __forceinline__ void flush_counts(unsigned long long* stats, const Counts& c, unsigned pixels) {
+    unsigned prim = __reduce_add_sync(0xffffffffu, c.primary);
+    unsigned light = __reduce_add_sync(0xffffffffu, c.light);
+    unsigned rays = __reduce_add_sync(0xffffffffu, c.rays);
+    unsigned pix = __reduce_add_sync(0xffffffffu, pixels);
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(stats + 0, (unsigned long long)prim);
+        atomicAdd(stats + 1, (unsigned long long)light);
+        atomicAdd(stats + 2, (unsigned long long)rays);
+        atomicAdd(stats + 3, (unsigned long long)pix);
+    }
+}
+
+}  // namespace mt

@@ -746,6 +746,32 @@ template <class T> int render(const orc_volumes* v, const mt_camera_ubo* cam, co
     return 0;
 }
 
+// cloudRayMarch.comp:690-826 for a list of pixels (x, y pairs), each marched
+// as in a full-raymarch frame; for error statistics on a sample of a large frame.
+template <class T> int march_pixels(const orc_volumes* v, const mt_camera_ubo* cam, const mt_time_ubo* tm,
+                                    const mt_params* p, int W, int H, const int32_t* xy, long long n, T* rgba,
+                                    T* mask, int nthreads) {
+    if (!v || !cam || !tm || !p || !xy || !rgba || W <= 0 || H <= 0 || n < 0) return 1;
+    Frame<T> F = make_frame<T>(v, cam, cam, tm, p);
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+#pragma omp parallel for schedule(dynamic, 64)
+    for (long long i = 0; i < n; ++i) {
+        Counters cnt;
+        T m;
+        V4<T> c = march_pixel(F, xy[2 * i], xy[2 * i + 1], W, H, &m, cnt);
+        rgba[4 * i] = c.x;
+        rgba[4 * i + 1] = c.y;
+        rgba[4 * i + 2] = c.z;
+        rgba[4 * i + 3] = c.w;
+        if (mask) mask[i] = m;
+    }
+    return 0;
+}
+
 template <class T> int txaa(const mt_camera_ubo* cam, const mt_camera_ubo* cam_old, const mt_time_ubo* tm,
                             const mt_params* p, const T* cur, const T* hist, T* out, int W, int H, int nthreads) {
     if (!cam || !cam_old || !tm || !p || !cur || !hist || !out || W <= 0 || H <= 0) return 1;
@@ -807,6 +833,19 @@ __attribute__((visibility("default"))) int orc_txaa_f64(const mt_camera_ubo* cam
                                                         const mt_time_ubo* tm, const mt_params* p, const double* cur,
                                                         const double* hist, double* out, int W, int H, int nthreads) {
     return orc::txaa<double>(cam, cam_old, tm, p, cur, hist, out, W, H, nthreads);
+}
+
+__attribute__((visibility("default"))) int orc_march_pixels_f32(const orc_volumes* v, const mt_camera_ubo* cam,
+                                                                const mt_time_ubo* tm, const mt_params* p, int W,
+                                                                int H, const int32_t* xy, long long n, float* rgba,
+                                                                float* mask, int nthreads) {
+    return orc::march_pixels<float>(v, cam, tm, p, W, H, xy, n, rgba, mask, nthreads);
+}
+__attribute__((visibility("default"))) int orc_march_pixels_f64(const orc_volumes* v, const mt_camera_ubo* cam,
+                                                                const mt_time_ubo* tm, const mt_params* p, int W,
+                                                                int H, const int32_t* xy, long long n, double* rgba,
+                                                                double* mask, int nthreads) {
+    return orc::march_pixels<double>(v, cam, tm, p, W, H, xy, n, rgba, mask, nthreads);
 }
 
 // Single-function probes for the unit tests (float instantiation).

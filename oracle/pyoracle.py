@@ -62,6 +62,10 @@ def lib() -> C.CDLL:
             f = getattr(L, name)
             f.restype = C.c_int
             f.argtypes = [cam, cam, tm, par, P, P, P, C.c_int, C.c_int, C.c_int]
+        for name in ("orc_march_pixels_f32", "orc_march_pixels_f64"):
+            f = getattr(L, name)
+            f.restype = C.c_int
+            f.argtypes = [C.POINTER(OrcVolumes), cam, tm, par, C.c_int, C.c_int, P, C.c_longlong, P, P, C.c_int]
         L.orc_generate_volumes.restype = None
         L.orc_generate_volumes.argtypes = [C.c_uint64] + [P] * 12
         L.orc_wang.restype = C.c_uint32
@@ -146,6 +150,28 @@ def render(vol: Volumes, cam, cam_old, tm, params, prev, width: int, height: int
     if rc != 0:
         raise RuntimeError(f"orc_render failed ({rc})")
     return cur, mask, counters
+
+
+def march_pixels(vol: Volumes, cam, tm, params, width: int, height: int, xy: np.ndarray, dtype=np.float64,
+                 nthreads: int = 0):
+    """Full-raymarch colour and god-ray value of the listed pixels (xy: n x 2 int32)."""
+    xy = np.ascontiguousarray(xy, np.int32)
+    n = xy.shape[0]
+    rgba = np.zeros((n, 4), dtype)
+    mask = np.zeros(n, dtype)
+    fn = lib().orc_march_pixels_f32 if dtype == np.float32 else lib().orc_march_pixels_f64
+    v = vol.c()
+    rc = fn(C.byref(v), C.byref(cam), C.byref(tm), C.byref(params), width, height, _ptr(xy), n, _ptr(rgba),
+            _ptr(mask), nthreads)
+    if rc != 0:
+        raise RuntimeError(f"orc_march_pixels failed ({rc})")
+    return rgba, mask
+
+
+def volumes_16(vols: dict, storage: str) -> Volumes:
+    """The texel values of the half ('h16') or bfloat16 ('b16') copies, as float32 (exact)."""
+    conv = half_bits_to_float if storage == "h16" else bf16_bits_to_float
+    return Volumes(*(conv(vols[k + "_" + storage]) for k in ("base", "detail", "curl", "weather")))
 
 
 def txaa(cam, cam_old, tm, params, current, history, dtype=np.float32, nthreads: int = 0):
