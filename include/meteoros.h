@@ -158,7 +158,10 @@ typedef struct mt_tuning {
     int32_t march_lanes;  /* lanes that march one ray together: 1, 4, 8 or 16; 0 = chosen from the ray count */
     int32_t fused_resolve; /* mt_render_frame: 0 = reprojection, march, TXAA as three launches (default);
                             * 1 = march, then reprojection fused with TXAA */
-    int32_t _reserved[6];
+    int32_t batch_tile_w;  /* mt_render_batch: tile of rays a CTA takes at a time (default 16 x 8) */
+    int32_t batch_tile_h;
+    int32_t batch_lanes;   /* mt_render_batch: lanes per ray, 1, 4, 8 or 16 (default 1) */
+    int32_t _reserved[3];
 } mt_tuning;
 
 /* One view of a batched render (config 3). */
@@ -263,8 +266,18 @@ MT_API mt_status mt_txaa(mt_ctx* ctx, const mt_camera_ubo* camera, const mt_came
                          const float* history_rgba, float* out_rgba, int width, int height, void* stream);
 
 /* Many views, uneven sizes, one persistent launch (config 3).  `views` is a
- * host array; its image pointers are device pointers. */
+ * host array; its image pointers are device pointers.  All views share one
+ * storage.  Checkerboard views are reprojected first, then one persistent
+ * raymarch launch takes tiles of every view from a work counter; the whole
+ * batch is a CUDA graph launched on `stream`.  Results equal mt_render per view.
+ * Batches on one context run in call order, whatever their streams. */
 MT_API mt_status mt_render_batch(mt_ctx* ctx, const mt_view* views, int n_views, void* stream);
+
+/* Times mt_render_batch on these views for every tile shape in
+ * {8x8, 16x8, 16x16, 32x8} and lanes in {1, 4}, keeps the fastest in the
+ * context's tuning and returns it (the views are rendered several times). */
+MT_API mt_status mt_autotune_batch(mt_ctx* ctx, const mt_view* views, int n_views, void* stream,
+                                   mt_tuning* best);
 
 /* Counters accumulated by render calls made with MT_RENDER_COUNT since the
  * last reset.  Synchronises the stream. */

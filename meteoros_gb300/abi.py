@@ -106,7 +106,8 @@ class Stats(C.Structure):
 
 
 class Tuning(C.Structure):
-    _fields_ = [("march_lanes", C.c_int32), ("fused_resolve", C.c_int32), ("_reserved", C.c_int32 * 6)]
+    _fields_ = [("march_lanes", C.c_int32), ("fused_resolve", C.c_int32), ("batch_tile_w", C.c_int32),
+                ("batch_tile_h", C.c_int32), ("batch_lanes", C.c_int32), ("_reserved", C.c_int32 * 3)]
 
 
 class KernelTimes(C.Structure):
@@ -162,6 +163,7 @@ SIGNATURES = {
                           C.POINTER(Params), _P, _P, _P, C.c_int, C.c_int, _P]),
     "mt_render_batch": (C.c_int, [_P, C.POINTER(View), C.c_int, _P]),
     "mt_get_stats": (C.c_int, [_P, C.POINTER(Stats), C.c_int, _P]),
+    "mt_autotune_batch": (C.c_int, [_P, C.POINTER(View), C.c_int, _P, C.POINTER(Tuning)]),
     "mt_set_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
     "mt_get_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
     "mt_selftest_division": (C.c_int, [_P, _P, _P, _P, _P, C.c_int, _P]),

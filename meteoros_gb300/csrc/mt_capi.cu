@@ -8,6 +8,7 @@
 //                                                (Renderer.cpp:914-1086)
 // Errors: every entry point returns an mt_status and records a message that
 // mt_last_error() returns; no exception crosses the boundary.
+#include <algorithm>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -37,6 +38,21 @@ struct mt_ctx {
     bool ran[4] = {false, false, false, false};
     int march_lanes = 0;                      // step-parallel lanes per ray (mt_set_tuning); 0 = auto
     int fused_resolve = 0;                    // mt_render_frame: reprojection fused with TXAA
+    // mt_render_batch
+    int batch_tile_w = 16, batch_tile_h = 8, batch_lanes = 1;
+    mt::MarchArgs* d_views = nullptr;         // device view table
+    mt::BatchTile* d_tiles = nullptr;         // device tile list
+    unsigned* d_counter = nullptr;            // work counter
+    mt::MarchArgs* h_views[2] = {nullptr, nullptr};  // pinned staging, two slots used in turn
+    mt::BatchTile* h_tiles[2] = {nullptr, nullptr};
+    cudaEvent_t slot_done[2] = {nullptr, nullptr};   // the batch that last used the slot has finished
+    bool slot_pending[2] = {false, false};
+    int slot = 0;
+    size_t cap_views = 0, cap_tiles = 0;
+    cudaStream_t cap_stream = nullptr;        // private stream the batch graph is captured on
+    cudaGraphExec_t batch_exec = nullptr;
+    cudaEvent_t batch_done = nullptr;         // the last batch graph has finished
+    bool batch_pending = false;
 };
 
 namespace {
@@ -243,6 +259,18 @@ MT_API void mt_destroy(mt_ctx* ctx) {
     cudaFree(ctx->stats);
     for (cudaEvent_t e : ctx->ev)
         if (e) cudaEventDestroy(e);
+    if (ctx->batch_pending) cudaEventSynchronize(ctx->batch_done);
+    cudaFree(ctx->d_views);
+    cudaFree(ctx->d_tiles);
+    cudaFree(ctx->d_counter);
+    for (int k = 0; k < 2; ++k) {
+        cudaFreeHost(ctx->h_views[k]);
+        cudaFreeHost(ctx->h_tiles[k]);
+        if (ctx->slot_done[k]) cudaEventDestroy(ctx->slot_done[k]);
+    }
+    if (ctx->batch_exec) cudaGraphExecDestroy(ctx->batch_exec);
+    if (ctx->cap_stream) cudaStreamDestroy(ctx->cap_stream);
+    if (ctx->batch_done) cudaEventDestroy(ctx->batch_done);
     delete ctx;
 }
 
@@ -439,16 +467,217 @@ MT_API mt_status mt_txaa(mt_ctx* ctx, const mt_camera_ubo* camera, const mt_came
     return MT_OK;
 }
 
+namespace {
+
+mt_status ensure_batch_buffers(mt_ctx* ctx, size_t n_views, size_t n_tiles) {
+    if (!ctx->cap_stream) {
+        MT_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->cap_stream, cudaStreamNonBlocking));
+        MT_CUDA(ctx, cudaEventCreateWithFlags(&ctx->batch_done, cudaEventDisableTiming));
+        for (int k = 0; k < 2; ++k) MT_CUDA(ctx, cudaEventCreateWithFlags(&ctx->slot_done[k], cudaEventDisableTiming));
+        MT_CUDA(ctx, cudaMalloc((void**)&ctx->d_counter, sizeof(unsigned)));
+    }
+    if (n_views > ctx->cap_views || n_tiles > ctx->cap_tiles) {
+        // Nothing in flight may still read the old buffers.
+        if (ctx->batch_pending) MT_CUDA(ctx, cudaEventSynchronize(ctx->batch_done));
+    }
+    if (n_views > ctx->cap_views) {
+        cudaFree(ctx->d_views);
+        ctx->d_views = nullptr;
+        for (int k = 0; k < 2; ++k) {
+            cudaFreeHost(ctx->h_views[k]);
+            ctx->h_views[k] = nullptr;
+        }
+        ctx->cap_views = 0;
+        const size_t cap = std::max<size_t>(n_views, 64);
+        MT_CUDA(ctx, cudaMalloc((void**)&ctx->d_views, cap * sizeof(mt::MarchArgs)));
+        for (int k = 0; k < 2; ++k)
+            MT_CUDA(ctx, cudaHostAlloc((void**)&ctx->h_views[k], cap * sizeof(mt::MarchArgs), cudaHostAllocDefault));
+        ctx->cap_views = cap;
+    }
+    if (n_tiles > ctx->cap_tiles) {
+        cudaFree(ctx->d_tiles);
+        ctx->d_tiles = nullptr;
+        for (int k = 0; k < 2; ++k) {
+            cudaFreeHost(ctx->h_tiles[k]);
+            ctx->h_tiles[k] = nullptr;
+        }
+        ctx->cap_tiles = 0;
+        const size_t cap = std::max<size_t>(n_tiles, 4096);
+        MT_CUDA(ctx, cudaMalloc((void**)&ctx->d_tiles, cap * sizeof(mt::BatchTile)));
+        for (int k = 0; k < 2; ++k)
+            MT_CUDA(ctx, cudaHostAlloc((void**)&ctx->h_tiles[k], cap * sizeof(mt::BatchTile), cudaHostAllocDefault));
+        ctx->cap_tiles = cap;
+    }
+    return MT_OK;
+}
+
+// The ray grid of a view: pixels (full) or the 4x4 blocks whose slot pixel
+// lies in the image and in the reference's dispatch (checkerboard).
+void ray_grid(const mt::MarchArgs& a, int* nrx, int* nry) {
+    if (a.flags & MT_RENDER_FULL) {
+        *nrx = a.width;
+        *nry = a.height;
+        return;
+    }
+    const int id = a.time.frame_count_mod16;
+    const int sx = a.params.slot_x[id], sy = a.params.slot_y[id];
+    *nrx = a.width > sx ? std::min(a.groups_x, (a.width - sx + 3) / 4) : 0;
+    *nry = a.height > sy ? std::min(a.groups_y, (a.height - sy + 3) / 4) : 0;
+}
+
+}  // namespace
+
 MT_API mt_status mt_render_batch(mt_ctx* ctx, const mt_view* views, int n_views, void* stream) {
     if (!ctx) return MT_ERR_INVALID_ARG;
     if (n_views < 0 || (n_views > 0 && !views)) return fail(ctx, MT_ERR_INVALID_ARG, "bad view list");
+    if (n_views == 0) return MT_OK;
+    mt_status st;
+    if ((st = bind_device(ctx)) != MT_OK) return st;
+    std::vector<mt::MarchArgs> args((size_t)n_views);
+    bool count = false;
     for (int i = 0; i < n_views; ++i) {
         const mt_view& v = views[i];
-        mt_status st = mt_render(ctx, &v.camera, &v.camera_old, &v.time, &v.params, v.prev_rgba, v.cur_rgba,
-                                 v.godray_mask, v.width, v.height, v.flags, stream);
-        if (st != MT_OK) return st;
+        st = build_march_args(ctx, &v.camera, &v.camera_old, &v.time, &v.params, v.prev_rgba, v.cur_rgba,
+                              v.godray_mask, v.width, v.height, v.flags, &args[(size_t)i]);
+        if (st != MT_OK) {
+            std::string m = ctx->err;
+            return fail(ctx, st, "view %d: %s", i, m.c_str());
+        }
+        if (v.params.storage != views[0].params.storage)
+            return fail(ctx, MT_ERR_INVALID_ARG, "view %d: all views of a batch must share one storage", i);
+        count = count || (v.flags & MT_RENDER_COUNT);
     }
+    // Tiles, most expensive views first (rays x steps), so the persistent
+    // launch does not end on one large view.
+    const int tw = ctx->batch_tile_w, th = ctx->batch_tile_h;
+    std::vector<int> order((size_t)n_views);
+    for (int i = 0; i < n_views; ++i) order[(size_t)i] = i;
+    auto cost = [&](int i) {
+        int nx, ny;
+        ray_grid(args[(size_t)i], &nx, &ny);
+        return (double)nx * ny * std::max(args[(size_t)i].params.steps_min, args[(size_t)i].params.steps_max);
+    };
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost(x) > cost(y); });
+    std::vector<mt::BatchTile> tiles;
+    for (int i : order) {
+        int nx, ny;
+        ray_grid(args[(size_t)i], &nx, &ny);
+        for (int y = 0; y < ny; y += th)
+            for (int x = 0; x < nx; x += tw) tiles.push_back(mt::BatchTile{i, x, y, nx, ny});
+    }
+    if ((st = ensure_batch_buffers(ctx, (size_t)n_views, tiles.size())) != MT_OK) return st;
+    // Staging slot: the batch that used it last (two calls ago) must have
+    // copied it out, i.e. finished.
+    const int k = ctx->slot;
+    ctx->slot ^= 1;
+    if (ctx->slot_pending[k]) MT_CUDA(ctx, cudaEventSynchronize(ctx->slot_done[k]));
+    mt::MarchArgs* h_views = ctx->h_views[k];
+    mt::BatchTile* h_tiles = ctx->h_tiles[k];
+    std::memcpy(h_views, args.data(), args.size() * sizeof(mt::MarchArgs));
+    if (!tiles.empty()) std::memcpy(h_tiles, tiles.data(), tiles.size() * sizeof(mt::BatchTile));
+
+    mt::BatchArgs b;
+    b.views = ctx->d_views;
+    b.tiles = ctx->d_tiles;
+    b.counter = ctx->d_counter;
+    b.stats = count ? ctx->stats : nullptr;
+    b.n_tiles = (int32_t)tiles.size();
+    b.tile_w = tw;
+    b.tile_h = th;
+    const int storage = views[0].params.storage;
+    const int lanes = ctx->batch_lanes;
+    int blocks = storage == MT_STORAGE_F16    ? mt::batch_blocks_f16(ctx->device, lanes)
+                 : storage == MT_STORAGE_BF16 ? mt::batch_blocks_bf16(ctx->device, lanes)
+                                              : mt::batch_blocks_u8(ctx->device, lanes);
+
+    cudaGraph_t graph = nullptr;
+    cudaStream_t cs = ctx->cap_stream;
+    MT_CUDA(ctx, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaMemcpyAsync(ctx->d_views, h_views, args.size() * sizeof(mt::MarchArgs),
+                                    cudaMemcpyHostToDevice, cs);
+    if (e == cudaSuccess && !tiles.empty())
+        e = cudaMemcpyAsync(ctx->d_tiles, h_tiles, tiles.size() * sizeof(mt::BatchTile), cudaMemcpyHostToDevice, cs);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_counter, 0, sizeof(unsigned), cs);
+    for (int i = 0; e == cudaSuccess && i < n_views; ++i)
+        if (!(args[(size_t)i].flags & MT_RENDER_FULL)) e = mt::launch_reproject(args[(size_t)i], cs);
+    if (e == cudaSuccess && !tiles.empty()) {
+        e = storage == MT_STORAGE_F16    ? mt::launch_batch_f16(b, lanes, blocks, cs)
+            : storage == MT_STORAGE_BF16 ? mt::launch_batch_bf16(b, lanes, blocks, cs)
+                                         : mt::launch_batch_u8(b, lanes, blocks, cs);
+    }
+    cudaError_t e_end = cudaStreamEndCapture(cs, &graph);
+    if (e != cudaSuccess || e_end != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return fail(ctx, MT_ERR_CUDA, "batch graph capture failed: %s",
+                    cudaGetErrorString(e != cudaSuccess ? e : e_end));
+    }
+    bool updated = false;
+    if (ctx->batch_exec) {
+        cudaGraphExecUpdateResultInfo info;
+        updated = cudaGraphExecUpdate(ctx->batch_exec, graph, &info) == cudaSuccess;
+        if (!updated) {
+            cudaGetLastError();
+            cudaGraphExecDestroy(ctx->batch_exec);
+            ctx->batch_exec = nullptr;
+        }
+    }
+    if (!updated) {
+        e = cudaGraphInstantiate(&ctx->batch_exec, graph, 0);
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(graph);
+            return fail(ctx, MT_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
+        }
+    }
+    cudaGraphDestroy(graph);
+    // Batches run in call order: wait for the previous one whatever its stream.
+    if (ctx->batch_pending) MT_CUDA(ctx, cudaStreamWaitEvent((cudaStream_t)stream, ctx->batch_done, 0));
+    MT_CUDA(ctx, cudaGraphLaunch(ctx->batch_exec, (cudaStream_t)stream));
+    MT_CUDA(ctx, cudaEventRecord(ctx->batch_done, (cudaStream_t)stream));
+    MT_CUDA(ctx, cudaEventRecord(ctx->slot_done[k], (cudaStream_t)stream));
+    ctx->batch_pending = true;
+    ctx->slot_pending[k] = true;
     return MT_OK;
+}
+
+MT_API mt_status mt_autotune_batch(mt_ctx* ctx, const mt_view* views, int n_views, void* stream, mt_tuning* best) {
+    if (!ctx) return MT_ERR_INVALID_ARG;
+    if (!best) return fail(ctx, MT_ERR_INVALID_ARG, "best must not be NULL");
+    mt_status st;
+    if ((st = bind_device(ctx)) != MT_OK) return st;
+    const int shapes[4][2] = {{8, 8}, {16, 8}, {16, 16}, {32, 8}};
+    const int lane_choices[2] = {1, 4};
+    cudaEvent_t t0, t1;
+    MT_CUDA(ctx, cudaEventCreate(&t0));
+    MT_CUDA(ctx, cudaEventCreate(&t1));
+    float best_ms = -1.0f;
+    int bw = ctx->batch_tile_w, bh = ctx->batch_tile_h, bl = ctx->batch_lanes;
+    st = mt_render_batch(ctx, views, n_views, stream);  // warm-up
+    for (int li = 0; st == MT_OK && li < 2; ++li)
+        for (int si = 0; st == MT_OK && si < 4; ++si) {
+            ctx->batch_tile_w = shapes[si][0];
+            ctx->batch_tile_h = shapes[si][1];
+            ctx->batch_lanes = lane_choices[li];
+            cudaEventRecord(t0, (cudaStream_t)stream);
+            st = mt_render_batch(ctx, views, n_views, stream);
+            cudaEventRecord(t1, (cudaStream_t)stream);
+            if (st != MT_OK) break;
+            float ms = 0.0f;
+            cudaEventSynchronize(t1);
+            cudaEventElapsedTime(&ms, t0, t1);
+            if (best_ms < 0.0f || ms < best_ms) {
+                best_ms = ms;
+                bw = shapes[si][0];
+                bh = shapes[si][1];
+                bl = lane_choices[li];
+            }
+        }
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    ctx->batch_tile_w = bw;
+    ctx->batch_tile_h = bh;
+    ctx->batch_lanes = bl;
+    if (st != MT_OK) return st;
+    return mt_get_tuning(ctx, best);
 }
 
 MT_API mt_status mt_get_stats(mt_ctx* ctx, mt_stats* out, int reset, void* stream) {
@@ -476,8 +705,15 @@ MT_API mt_status mt_set_tuning(mt_ctx* ctx, const mt_tuning* t) {
                     t->march_lanes);
     if (t->fused_resolve != 0 && t->fused_resolve != 1)
         return fail(ctx, MT_ERR_INVALID_ARG, "fused_resolve must be 0 or 1");
+    if (t->batch_tile_w < 1 || t->batch_tile_h < 1 || t->batch_tile_w * t->batch_tile_h > 4096)
+        return fail(ctx, MT_ERR_INVALID_ARG, "batch tile must be 1..4096 rays");
+    if (t->batch_lanes != 1 && t->batch_lanes != 4 && t->batch_lanes != 8 && t->batch_lanes != 16)
+        return fail(ctx, MT_ERR_INVALID_ARG, "batch_lanes must be 1, 4, 8 or 16");
     ctx->march_lanes = t->march_lanes;
     ctx->fused_resolve = t->fused_resolve;
+    ctx->batch_tile_w = t->batch_tile_w;
+    ctx->batch_tile_h = t->batch_tile_h;
+    ctx->batch_lanes = t->batch_lanes;
     return MT_OK;
 }
 
@@ -487,6 +723,9 @@ MT_API mt_status mt_get_tuning(mt_ctx* ctx, mt_tuning* t) {
     std::memset(t, 0, sizeof(*t));
     t->march_lanes = ctx->march_lanes;
     t->fused_resolve = ctx->fused_resolve;
+    t->batch_tile_w = ctx->batch_tile_w;
+    t->batch_tile_h = ctx->batch_tile_h;
+    t->batch_lanes = ctx->batch_lanes;
     return MT_OK;
 }
 

@@ -43,6 +43,24 @@ struct TxaaArgs {
     int32_t width, height;
 };
 
+// One tile of a batched render: a TW x TH rectangle of one view's ray grid.
+struct BatchTile {
+    int32_t view;      // index into BatchArgs::views
+    int32_t rx0, ry0;  // tile origin in the view's ray grid
+    int32_t nrx, nry;  // the view's ray grid: pixels (full) or 4x4 blocks (checkerboard)
+};
+
+// A batch of views marched by one persistent launch: every CTA takes tiles
+// from `counter` (zeroed before the launch) until all are done.
+struct BatchArgs {
+    const MarchArgs* views;  // device array, one per view
+    const BatchTile* tiles;  // device array, in the order they are handed out
+    unsigned* counter;
+    unsigned long long* stats;  // or NULL
+    int32_t n_tiles;
+    int32_t tile_w, tile_h;     // tile shape in rays
+};
+
 // Outputs of one generator launch (any pointer may be NULL).
 struct NoiseOut {
     uint32_t* u8;   // RGBA8 words
@@ -59,7 +77,16 @@ struct LaunchEvents {
 };
 
 cudaError_t launch_render(const MarchArgs& a, cudaStream_t s, const LaunchEvents* ev);
+cudaError_t launch_reproject(const MarchArgs& a, cudaStream_t s);
 cudaError_t launch_march_u8(const MarchArgs& a, cudaStream_t s, long long rays);
+// Persistent batched march: `blocks` CTAs of 128 threads, `lanes` per ray.
+cudaError_t launch_batch_u8(const BatchArgs& b, int lanes, int blocks, cudaStream_t s);
+cudaError_t launch_batch_f16(const BatchArgs& b, int lanes, int blocks, cudaStream_t s);
+cudaError_t launch_batch_bf16(const BatchArgs& b, int lanes, int blocks, cudaStream_t s);
+// CTAs of the persistent batched march that fit on the device at once.
+int batch_blocks_u8(int device, int lanes);
+int batch_blocks_f16(int device, int lanes);
+int batch_blocks_bf16(int device, int lanes);
 cudaError_t launch_march_f16(const MarchArgs& a, cudaStream_t s, long long rays);
 cudaError_t launch_march_bf16(const MarchArgs& a, cudaStream_t s, long long rays);
 cudaError_t launch_txaa(const TxaaArgs& a, cudaStream_t s, const cudaEvent_t* ev);

@@ -343,6 +343,71 @@ __global__ void __launch_bounds__(128, 8) march_kernel(const __grid_constant__ M
 }
 
 
+// Batched form (config 3): one persistent launch over many views of uneven
+// size.  Each CTA repeatedly takes the next tile from the batch's counter and
+// marches its rays, 128/G rays per pass; per-view arguments come from the
+// view table in global memory.  Per-pixel results equal those of separate
+// march_kernel launches (the same march_pixel runs on the same inputs).
+template <int G, int S>
+__global__ void __launch_bounds__(128, 8) march_batch_kernel(const __grid_constant__ BatchArgs b) {
+    __shared__ int s_tile;
+    using T = typename Vol<S>::T;
+    const int lane = (int)(threadIdx.x % G);
+    const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
+    constexpr int kRaysPerPass = 128 / G;
+    Counts cnt{0u, 0u, 0u};
+    unsigned pixels = 0;
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = (int)atomicAdd(b.counter, 1u);
+        __syncthreads();
+        const int t = s_tile;
+        __syncthreads();
+        if (t >= b.n_tiles) break;
+        const BatchTile tile = b.tiles[t];
+        const MarchArgs& a = b.views[tile.view];
+        const Frame F = make_frame(a.params);
+        const Tex<S> tx{(const T*)a.vol[0], (const T*)a.vol[1], (const T*)a.vol[2], (const T*)a.vol[3]};
+        const bool full = (a.flags & MT_RENDER_FULL) != 0;
+        const int id = a.time.frame_count_mod16;
+        const int sx = full ? 0 : a.params.slot_x[id], sy = full ? 0 : a.params.slot_y[id];
+        const int step = full ? 1 : 4;
+        const int tile_rays = b.tile_w * b.tile_h;
+        for (int r0 = 0; r0 < tile_rays; r0 += kRaysPerPass) {
+            const int r = r0 + (int)(threadIdx.x / G);
+            const int rx = tile.rx0 + r % b.tile_w, ry = tile.ry0 + r / b.tile_w;
+            const int px = rx * step + sx, py = ry * step + sy;
+            const bool active = r < tile_rays && rx < tile.nrx && ry < tile.nry && px < a.width && py < a.height;
+            if (active) {
+                march_pixel<G, S>(a, F, tx, px, py, cnt, gmask, lane);
+                pixels += lane == 0 ? 1u : 0u;
+            }
+        }
+    }
+    if (b.stats) flush_counts(b.stats, cnt, pixels);
+}
+
+template <int S> cudaError_t launch_batch_storage(const BatchArgs& b, int lanes, int blocks, cudaStream_t s) {
+    switch (lanes) {
+        case 1: march_batch_kernel<1, S><<<blocks, 128, 0, s>>>(b); break;
+        case 4: march_batch_kernel<4, S><<<blocks, 128, 0, s>>>(b); break;
+        case 16: march_batch_kernel<16, S><<<blocks, 128, 0, s>>>(b); break;
+        default: march_batch_kernel<8, S><<<blocks, 128, 0, s>>>(b); break;
+    }
+    return cudaGetLastError();
+}
+
+template <int S> int batch_blocks_storage(int device, int lanes) {
+    int per_sm = 0, sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    switch (lanes) {
+        case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, march_batch_kernel<1, S>, 128, 0); break;
+        case 4: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, march_batch_kernel<4, S>, 128, 0); break;
+        case 16: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, march_batch_kernel<16, S>, 128, 0); break;
+        default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, march_batch_kernel<8, S>, 128, 0); break;
+    }
+    return (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
+}
+
 template <int S> cudaError_t launch_march_storage(const MarchArgs& a, cudaStream_t s, long long rays) {
     const int G = a.lanes;
     const unsigned blocks = (unsigned)((rays * G + 127) / 128);

@@ -5,4 +5,8 @@ namespace mt {
 cudaError_t launch_march_u8(const MarchArgs& a, cudaStream_t s, long long rays) {
     return launch_march_storage<MT_STORAGE_U8>(a, s, rays);
 }
+cudaError_t launch_batch_u8(const BatchArgs& b, int lanes, int blocks, cudaStream_t s) {
+    return launch_batch_storage<MT_STORAGE_U8>(b, lanes, blocks, s);
+}
+int batch_blocks_u8(int device, int lanes) { return batch_blocks_storage<MT_STORAGE_U8>(device, lanes); }
 }  // namespace mt

@@ -249,14 +249,18 @@ static cudaError_t launch_march(const MarchArgs& a, cudaStream_t s, const Launch
     return e != cudaSuccess ? e : cudaGetLastError();
 }
 
+cudaError_t launch_reproject(const MarchArgs& a, cudaStream_t s) {
+    const long long n = (long long)a.width * a.height;
+    reproject_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_render(const MarchArgs& a, cudaStream_t s, const LaunchEvents* ev) {
     const bool timed = ev && ev->on;
     if (!(a.flags & MT_RENDER_FULL)) {
-        const long long n = (long long)a.width * a.height;
         if (timed) cudaEventRecord(ev->reproject[0], s);
-        reproject_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a);
+        cudaError_t e = launch_reproject(a, s);
         if (timed) cudaEventRecord(ev->reproject[1], s);
-        cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
     return launch_march(a, s, ev);

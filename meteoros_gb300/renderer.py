@@ -131,13 +131,24 @@ class Context:
         arr = (abi.View * len(views))(*views)
         self._check(self.lib.mt_render_batch(self.handle, arr, len(views), _stream(stream)))
 
-    def set_tuning(self, march_lanes: int | None = None, fused_resolve: bool | None = None) -> abi.Tuning:
+    def autotune_batch(self, views: list[abi.View], stream=None) -> abi.Tuning:
+        arr = (abi.View * len(views))(*views)
+        t = abi.Tuning()
+        self._check(self.lib.mt_autotune_batch(self.handle, arr, len(views), _stream(stream), C.byref(t)))
+        return t
+
+    def set_tuning(self, march_lanes: int | None = None, fused_resolve: bool | None = None,
+                   batch_tile: tuple[int, int] | None = None, batch_lanes: int | None = None) -> abi.Tuning:
         t = abi.Tuning()
         self._check(self.lib.mt_get_tuning(self.handle, C.byref(t)))
         if march_lanes is not None:
             t.march_lanes = march_lanes
         if fused_resolve is not None:
             t.fused_resolve = 1 if fused_resolve else 0
+        if batch_tile is not None:
+            t.batch_tile_w, t.batch_tile_h = batch_tile
+        if batch_lanes is not None:
+            t.batch_lanes = batch_lanes
         self._check(self.lib.mt_set_tuning(self.handle, C.byref(t)))
         return t
 

@@ -91,3 +91,33 @@ def C_copy(dst, src):
 
     ctypes.memmove(ctypes.addressof(dst), ctypes.addressof(src), ctypes.sizeof(src))
     return dst
+
+
+CONFIG3_RESOLUTIONS = ((256, 256), (640, 360), (960, 540), (1280, 720), (1920, 1080))
+
+
+def config3_views(seed: int, n_views: int = 64, resolutions=CONFIG3_RESOLUTIONS):
+    """The batched workload (config 3): per view a resolution drawn uniformly
+    from `resolutions`, a camera/sun/time drawn as in config 0, a step budget
+    drawn from U{64..128} and its own weather map (generated from seed + view
+    id into weather slot view id).  Returns [(width, height, camera, time, params)]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for v in range(n_views):
+        w, h = resolutions[int(rng.integers(0, len(resolutions)))]
+        cam, tm, params, _ = config_view(seed * 1000 + v, w, h, steps=int(rng.integers(64, 129)))
+        params.weather_slot = v
+        out.append((w, h, cam, tm, params))
+    return out
+
+
+def make_view(cam, cam_old, tm, params, cur, prev=None, mask=None, flags: int = 1) -> abi.View:
+    """An mt_view over device tensors (cur/prev: (H, W, 4) float32, mask: (H, W))."""
+    v = abi.View()
+    v.camera, v.camera_old, v.time, v.params = cam, cam_old, tm, params
+    v.prev_rgba = None if prev is None else prev.data_ptr()
+    v.cur_rgba = cur.data_ptr()
+    v.godray_mask = None if mask is None else mask.data_ptr()
+    v.height, v.width = int(cur.shape[0]), int(cur.shape[1])
+    v.flags = flags
+    return v
