@@ -270,7 +270,9 @@ MT_API mt_status mt_txaa(mt_ctx* ctx, const mt_camera_ubo* camera, const mt_came
  * storage.  Checkerboard views are reprojected first, then one persistent
  * raymarch launch takes tiles of every view from a work counter; the whole
  * batch is a CUDA graph launched on `stream`.  Results equal mt_render per view.
- * Batches on one context run in call order, whatever their streams. */
+ * Two batches may be in flight at once (on two streams they overlap on the
+ * device); a third waits for the first.  The views' images of batches in
+ * flight together must not overlap. */
 MT_API mt_status mt_render_batch(mt_ctx* ctx, const mt_view* views, int n_views, void* stream);
 
 /* Times mt_render_batch on these views for every tile shape in

@@ -40,19 +40,18 @@ struct mt_ctx {
     int fused_resolve = 0;                    // mt_render_frame: reprojection fused with TXAA
     // mt_render_batch
     int batch_tile_w = 16, batch_tile_h = 8, batch_lanes = 1;
-    mt::MarchArgs* d_views = nullptr;         // device view table
-    mt::BatchTile* d_tiles = nullptr;         // device tile list
-    unsigned* d_counter = nullptr;            // work counter
+    // Two slots used in turn, so two batches may run at once on two streams.
+    mt::MarchArgs* d_views[2] = {nullptr, nullptr};  // device view tables
+    mt::BatchTile* d_tiles[2] = {nullptr, nullptr};  // device tile lists
+    unsigned* d_counter[2] = {nullptr, nullptr};     // work counters
     mt::MarchArgs* h_views[2] = {nullptr, nullptr};  // pinned staging, two slots used in turn
     mt::BatchTile* h_tiles[2] = {nullptr, nullptr};
     cudaEvent_t slot_done[2] = {nullptr, nullptr};   // the batch that last used the slot has finished
     bool slot_pending[2] = {false, false};
     int slot = 0;
     size_t cap_views = 0, cap_tiles = 0;
-    cudaStream_t cap_stream = nullptr;        // private stream the batch graph is captured on
-    cudaGraphExec_t batch_exec = nullptr;
-    cudaEvent_t batch_done = nullptr;         // the last batch graph has finished
-    bool batch_pending = false;
+    cudaStream_t cap_stream = nullptr;        // private stream the batch graphs are captured on
+    cudaGraphExec_t batch_exec[2] = {nullptr, nullptr};
 };
 
 namespace {
@@ -259,18 +258,17 @@ MT_API void mt_destroy(mt_ctx* ctx) {
     cudaFree(ctx->stats);
     for (cudaEvent_t e : ctx->ev)
         if (e) cudaEventDestroy(e);
-    if (ctx->batch_pending) cudaEventSynchronize(ctx->batch_done);
-    cudaFree(ctx->d_views);
-    cudaFree(ctx->d_tiles);
-    cudaFree(ctx->d_counter);
     for (int k = 0; k < 2; ++k) {
+        if (ctx->slot_pending[k]) cudaEventSynchronize(ctx->slot_done[k]);
+        cudaFree(ctx->d_views[k]);
+        cudaFree(ctx->d_tiles[k]);
+        cudaFree(ctx->d_counter[k]);
         cudaFreeHost(ctx->h_views[k]);
         cudaFreeHost(ctx->h_tiles[k]);
         if (ctx->slot_done[k]) cudaEventDestroy(ctx->slot_done[k]);
+        if (ctx->batch_exec[k]) cudaGraphExecDestroy(ctx->batch_exec[k]);
     }
-    if (ctx->batch_exec) cudaGraphExecDestroy(ctx->batch_exec);
     if (ctx->cap_stream) cudaStreamDestroy(ctx->cap_stream);
-    if (ctx->batch_done) cudaEventDestroy(ctx->batch_done);
     delete ctx;
 }
 
@@ -472,40 +470,44 @@ namespace {
 mt_status ensure_batch_buffers(mt_ctx* ctx, size_t n_views, size_t n_tiles) {
     if (!ctx->cap_stream) {
         MT_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->cap_stream, cudaStreamNonBlocking));
-        MT_CUDA(ctx, cudaEventCreateWithFlags(&ctx->batch_done, cudaEventDisableTiming));
-        for (int k = 0; k < 2; ++k) MT_CUDA(ctx, cudaEventCreateWithFlags(&ctx->slot_done[k], cudaEventDisableTiming));
-        MT_CUDA(ctx, cudaMalloc((void**)&ctx->d_counter, sizeof(unsigned)));
+        for (int k = 0; k < 2; ++k) {
+            MT_CUDA(ctx, cudaEventCreateWithFlags(&ctx->slot_done[k], cudaEventDisableTiming));
+            MT_CUDA(ctx, cudaMalloc((void**)&ctx->d_counter[k], sizeof(unsigned)));
+        }
     }
     if (n_views > ctx->cap_views || n_tiles > ctx->cap_tiles) {
         // Nothing in flight may still read the old buffers.
-        if (ctx->batch_pending) MT_CUDA(ctx, cudaEventSynchronize(ctx->batch_done));
+        for (int k = 0; k < 2; ++k)
+            if (ctx->slot_pending[k]) MT_CUDA(ctx, cudaEventSynchronize(ctx->slot_done[k]));
     }
     if (n_views > ctx->cap_views) {
-        cudaFree(ctx->d_views);
-        ctx->d_views = nullptr;
+        const size_t cap = std::max<size_t>(n_views, 64);
         for (int k = 0; k < 2; ++k) {
+            cudaFree(ctx->d_views[k]);
             cudaFreeHost(ctx->h_views[k]);
+            ctx->d_views[k] = nullptr;
             ctx->h_views[k] = nullptr;
         }
         ctx->cap_views = 0;
-        const size_t cap = std::max<size_t>(n_views, 64);
-        MT_CUDA(ctx, cudaMalloc((void**)&ctx->d_views, cap * sizeof(mt::MarchArgs)));
-        for (int k = 0; k < 2; ++k)
+        for (int k = 0; k < 2; ++k) {
+            MT_CUDA(ctx, cudaMalloc((void**)&ctx->d_views[k], cap * sizeof(mt::MarchArgs)));
             MT_CUDA(ctx, cudaHostAlloc((void**)&ctx->h_views[k], cap * sizeof(mt::MarchArgs), cudaHostAllocDefault));
+        }
         ctx->cap_views = cap;
     }
     if (n_tiles > ctx->cap_tiles) {
-        cudaFree(ctx->d_tiles);
-        ctx->d_tiles = nullptr;
+        const size_t cap = std::max<size_t>(n_tiles, 4096);
         for (int k = 0; k < 2; ++k) {
+            cudaFree(ctx->d_tiles[k]);
             cudaFreeHost(ctx->h_tiles[k]);
+            ctx->d_tiles[k] = nullptr;
             ctx->h_tiles[k] = nullptr;
         }
         ctx->cap_tiles = 0;
-        const size_t cap = std::max<size_t>(n_tiles, 4096);
-        MT_CUDA(ctx, cudaMalloc((void**)&ctx->d_tiles, cap * sizeof(mt::BatchTile)));
-        for (int k = 0; k < 2; ++k)
+        for (int k = 0; k < 2; ++k) {
+            MT_CUDA(ctx, cudaMalloc((void**)&ctx->d_tiles[k], cap * sizeof(mt::BatchTile)));
             MT_CUDA(ctx, cudaHostAlloc((void**)&ctx->h_tiles[k], cap * sizeof(mt::BatchTile), cudaHostAllocDefault));
+        }
         ctx->cap_tiles = cap;
     }
     return MT_OK;
@@ -566,8 +568,8 @@ MT_API mt_status mt_render_batch(mt_ctx* ctx, const mt_view* views, int n_views,
             for (int x = 0; x < nx; x += tw) tiles.push_back(mt::BatchTile{i, x, y, nx, ny});
     }
     if ((st = ensure_batch_buffers(ctx, (size_t)n_views, tiles.size())) != MT_OK) return st;
-    // Staging slot: the batch that used it last (two calls ago) must have
-    // copied it out, i.e. finished.
+    // Slot: the batch that used it last (two calls ago) must have finished
+    // before its staging is overwritten (host) and its tables reused (device).
     const int k = ctx->slot;
     ctx->slot ^= 1;
     if (ctx->slot_pending[k]) MT_CUDA(ctx, cudaEventSynchronize(ctx->slot_done[k]));
@@ -577,9 +579,9 @@ MT_API mt_status mt_render_batch(mt_ctx* ctx, const mt_view* views, int n_views,
     if (!tiles.empty()) std::memcpy(h_tiles, tiles.data(), tiles.size() * sizeof(mt::BatchTile));
 
     mt::BatchArgs b;
-    b.views = ctx->d_views;
-    b.tiles = ctx->d_tiles;
-    b.counter = ctx->d_counter;
+    b.views = ctx->d_views[k];
+    b.tiles = ctx->d_tiles[k];
+    b.counter = ctx->d_counter[k];
     b.stats = count ? ctx->stats : nullptr;
     b.n_tiles = (int32_t)tiles.size();
     b.tile_w = tw;
@@ -593,11 +595,12 @@ MT_API mt_status mt_render_batch(mt_ctx* ctx, const mt_view* views, int n_views,
     cudaGraph_t graph = nullptr;
     cudaStream_t cs = ctx->cap_stream;
     MT_CUDA(ctx, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-    cudaError_t e = cudaMemcpyAsync(ctx->d_views, h_views, args.size() * sizeof(mt::MarchArgs),
+    cudaError_t e = cudaMemcpyAsync(ctx->d_views[k], h_views, args.size() * sizeof(mt::MarchArgs),
                                     cudaMemcpyHostToDevice, cs);
     if (e == cudaSuccess && !tiles.empty())
-        e = cudaMemcpyAsync(ctx->d_tiles, h_tiles, tiles.size() * sizeof(mt::BatchTile), cudaMemcpyHostToDevice, cs);
-    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_counter, 0, sizeof(unsigned), cs);
+        e = cudaMemcpyAsync(ctx->d_tiles[k], h_tiles, tiles.size() * sizeof(mt::BatchTile), cudaMemcpyHostToDevice,
+                            cs);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_counter[k], 0, sizeof(unsigned), cs);
     for (int i = 0; e == cudaSuccess && i < n_views; ++i)
         if (!(args[(size_t)i].flags & MT_RENDER_FULL)) e = mt::launch_reproject(args[(size_t)i], cs);
     if (e == cudaSuccess && !tiles.empty()) {
@@ -612,29 +615,29 @@ MT_API mt_status mt_render_batch(mt_ctx* ctx, const mt_view* views, int n_views,
                     cudaGetErrorString(e != cudaSuccess ? e : e_end));
     }
     bool updated = false;
-    if (ctx->batch_exec) {
+    cudaGraphExec_t& exec = ctx->batch_exec[k];
+    if (exec) {
         cudaGraphExecUpdateResultInfo info;
-        updated = cudaGraphExecUpdate(ctx->batch_exec, graph, &info) == cudaSuccess;
+        updated = cudaGraphExecUpdate(exec, graph, &info) == cudaSuccess;
         if (!updated) {
             cudaGetLastError();
-            cudaGraphExecDestroy(ctx->batch_exec);
-            ctx->batch_exec = nullptr;
+            cudaGraphExecDestroy(exec);
+            exec = nullptr;
         }
     }
     if (!updated) {
-        e = cudaGraphInstantiate(&ctx->batch_exec, graph, 0);
+        e = cudaGraphInstantiate(&exec, graph, 0);
         if (e != cudaSuccess) {
             cudaGraphDestroy(graph);
             return fail(ctx, MT_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
         }
     }
     cudaGraphDestroy(graph);
-    // Batches run in call order: wait for the previous one whatever its stream.
-    if (ctx->batch_pending) MT_CUDA(ctx, cudaStreamWaitEvent((cudaStream_t)stream, ctx->batch_done, 0));
-    MT_CUDA(ctx, cudaGraphLaunch(ctx->batch_exec, (cudaStream_t)stream));
-    MT_CUDA(ctx, cudaEventRecord(ctx->batch_done, (cudaStream_t)stream));
+    // The slot's previous batch must be done with its device tables,
+    // whatever stream it ran on; batches in the other slot may overlap.
+    if (ctx->slot_pending[k]) MT_CUDA(ctx, cudaStreamWaitEvent((cudaStream_t)stream, ctx->slot_done[k], 0));
+    MT_CUDA(ctx, cudaGraphLaunch(exec, (cudaStream_t)stream));
     MT_CUDA(ctx, cudaEventRecord(ctx->slot_done[k], (cudaStream_t)stream));
-    ctx->batch_pending = true;
     ctx->slot_pending[k] = true;
     return MT_OK;
 }

@@ -98,3 +98,24 @@ def test_batch_rejects_mixed_storage_and_bad_views(ctx):
     with pytest.raises(abi.MeteorosError):
         ctx.render_batch(views)
     ctx.render_batch([])
+
+
+def test_batches_overlap_on_two_streams(ctx):
+    """Three batches over disjoint images on two streams (the second overlaps
+    the first on the device; the third reuses the first one's slot)."""
+    views, bufs = build_views()
+    want, _ = per_view(ctx, bufs)
+    for b in bufs:
+        b[4].fill_(float("nan"))
+        b[5].fill_(float("nan"))
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    s1.wait_stream(torch.cuda.current_stream())
+    s2.wait_stream(torch.cuda.current_stream())
+    ctx.render_batch(views[0:5], stream=s1)
+    ctx.render_batch(views[5:9], stream=s2)
+    ctx.render_batch(views[9:12], stream=s1)
+    torch.cuda.synchronize()
+    ctx.stats(reset=True)
+    for i, (b, (wc, wm)) in enumerate(zip(bufs, want)):
+        assert_bits_equal(b[4].cpu().numpy(), wc, f"view {i} rgba (two streams)")
+        assert_bits_equal(b[5].cpu().numpy(), wm, f"view {i} mask (two streams)")
