@@ -281,6 +281,27 @@ MT_API mt_status mt_render_batch(mt_ctx* ctx, const mt_view* views, int n_views,
 MT_API mt_status mt_autotune_batch(mt_ctx* ctx, const mt_view* views, int n_views, void* stream,
                                    mt_tuning* best);
 
+/* mt_render_batch without any device allocation.  No counterpart in the
+ * reference.  For callers that cannot allocate device memory on the render
+ * path: cudaMalloc and cudaFree synchronise the device and stall every other
+ * stream of a frame loop, and a host that has handed its HBM budget to its
+ * own pool has none left to give.  The view table, tile list and work
+ * counter live in one fixed device array of the library (about 0.7 MB):
+ * at most MT_NOALLOC_MAX_VIEWS views and MT_NOALLOC_MAX_TILES tiles of the
+ * context's batch tile shape; a batch beyond either limit is rejected with
+ * MT_ERR_INVALID_ARG.  No CUDA graph is used: the tables are copied on
+ * `stream`, then the reprojections and the persistent raymarch are launched
+ * on it.  Results equal mt_render_batch.
+ *
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * Every call on a device shares the one array and leaves its tables there:
+ * calls on one stream are ordered, but calls whose work may overlap on the
+ * device (two streams not ordered by events) race on the array. */
+#define MT_NOALLOC_MAX_VIEWS 64
+#define MT_NOALLOC_MAX_TILES 32768
+MT_API mt_status mt_render_batch_noalloc(mt_ctx* ctx, const mt_view* views, int n_views, void* stream);
+
 /* Counters accumulated by render calls made with MT_RENDER_COUNT since the
  * last reset.  Synchronises the stream. */
 MT_API mt_status mt_get_stats(mt_ctx* ctx, mt_stats* out, int reset, void* stream);

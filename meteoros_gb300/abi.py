@@ -20,6 +20,8 @@ MT_DETAIL_N = 32
 MT_CURL_N = 128
 MT_WEATHER_N = 512
 MT_MAX_WEATHER_SLOTS = 256
+MT_NOALLOC_MAX_VIEWS = 64
+MT_NOALLOC_MAX_TILES = 32768
 
 MT_OK = 0
 MT_ERR_INVALID_ARG = 1
@@ -164,6 +166,7 @@ SIGNATURES = {
     "mt_render_batch": (C.c_int, [_P, C.POINTER(View), C.c_int, _P]),
     "mt_get_stats": (C.c_int, [_P, C.POINTER(Stats), C.c_int, _P]),
     "mt_autotune_batch": (C.c_int, [_P, C.POINTER(View), C.c_int, _P, C.POINTER(Tuning)]),
+    "mt_render_batch_noalloc": (C.c_int, [_P, C.POINTER(View), C.c_int, _P]),
     "mt_set_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
     "mt_get_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
     "mt_selftest_division": (C.c_int, [_P, _P, _P, _P, _P, C.c_int, _P]),

@@ -12,6 +12,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -767,6 +768,145 @@ MT_API mt_status mt_get_kernel_times(mt_ctx* ctx, mt_kernel_times* out) {
         MT_CUDA(ctx, cudaEventSynchronize(ctx->ev[2 * k + 1]));
         MT_CUDA(ctx, cudaEventElapsedTime(dst[k], ctx->ev[2 * k], ctx->ev[2 * k + 1]));
     }
+    return MT_OK;
+}
+
+}  // extern "C"
+
+// ---- mt_render_batch_noalloc -------------------------------------------
+// The batched raymarch with its view table, tile list and work counter in one
+// fixed device array of this library instead of buffers the context
+// allocates.  Layout (bytes): [0, 256) work counter; [256, 256 + views)
+// MT_NOALLOC_MAX_VIEWS view tables; then MT_NOALLOC_MAX_TILES tiles.
+namespace {
+
+constexpr size_t kNoallocViewsOff = 256;
+constexpr size_t kNoallocViewsBytes =
+    ((MT_NOALLOC_MAX_VIEWS * sizeof(mt::MarchArgs) + 255) / 256) * 256;
+constexpr size_t kNoallocTilesOff = kNoallocViewsOff + kNoallocViewsBytes;
+constexpr size_t kNoallocBytes = kNoallocTilesOff + MT_NOALLOC_MAX_TILES * sizeof(mt::BatchTile);
+constexpr int kNoallocMaxDevices = 64;
+static_assert(alignof(mt::MarchArgs) <= 256 && alignof(mt::BatchTile) <= 256, "scratch layout");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
+
+// Host image of the array's counter + view region and its tile region,
+// filled under g_noalloc_mu and copied with cudaMemcpyAsync: a copy from
+// pageable memory is staged before the call returns, so the next call may
+// refill it at once.
+std::mutex g_noalloc_mu;
+unsigned char g_noalloc_host[kNoallocBytes];
+unsigned char* g_noalloc_dev[kNoallocMaxDevices] = {};
+
+// Address of the array on ctx->device (current); looked up on the first
+// call made on that device.
+mt_status noalloc_scratch(mt_ctx* ctx, unsigned char** out) {
+    if (ctx->device < 0 || ctx->device >= kNoallocMaxDevices)
+        return fail(ctx, MT_ERR_UNSUPPORTED, "device %d is beyond the %d devices of the fixed scratch table",
+                    ctx->device, kNoallocMaxDevices);
+    if (!g_noalloc_dev[ctx->device]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(ctx, MT_ERR_CUDA, "cudaGetSymbolAddress of the batch scratch: %s", cudaGetErrorString(e));
+        g_noalloc_dev[ctx->device] = static_cast<unsigned char*>(p);
+    }
+    *out = g_noalloc_dev[ctx->device];
+    return MT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+MT_API mt_status mt_render_batch_noalloc(mt_ctx* ctx, const mt_view* views, int n_views, void* stream) {
+    if (!ctx) return MT_ERR_INVALID_ARG;
+    if (n_views < 0 || (n_views > 0 && !views)) return fail(ctx, MT_ERR_INVALID_ARG, "bad view list");
+    if (n_views > MT_NOALLOC_MAX_VIEWS)
+        return fail(ctx, MT_ERR_INVALID_ARG, "%d views exceed the fixed table of %d views", n_views,
+                    MT_NOALLOC_MAX_VIEWS);
+    if (n_views == 0) return MT_OK;
+    mt_status st;
+    if ((st = bind_device(ctx)) != MT_OK) return st;
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    unsigned char* dev = nullptr;
+    if ((st = noalloc_scratch(ctx, &dev)) != MT_OK) return st;
+    mt::MarchArgs* args = reinterpret_cast<mt::MarchArgs*>(g_noalloc_host + kNoallocViewsOff);
+    mt::BatchTile* tiles = reinterpret_cast<mt::BatchTile*>(g_noalloc_host + kNoallocTilesOff);
+    bool count = false;
+    for (int i = 0; i < n_views; ++i) {
+        const mt_view& v = views[i];
+        st = build_march_args(ctx, &v.camera, &v.camera_old, &v.time, &v.params, v.prev_rgba, v.cur_rgba,
+                              v.godray_mask, v.width, v.height, v.flags, &args[i]);
+        if (st != MT_OK) {
+            const std::string m = ctx->err;
+            return fail(ctx, st, "view %d: %s", i, m.c_str());
+        }
+        if (v.params.storage != views[0].params.storage)
+            return fail(ctx, MT_ERR_INVALID_ARG, "view %d: all views of a batch must share one storage", i);
+        count = count || (v.flags & MT_RENDER_COUNT);
+    }
+    // Tiles, most expensive views first (insertion sort of at most
+    // MT_NOALLOC_MAX_VIEWS views, stable like mt_render_batch's order).
+    int order[MT_NOALLOC_MAX_VIEWS];
+    double cost[MT_NOALLOC_MAX_VIEWS];
+    for (int i = 0; i < n_views; ++i) {
+        int nx, ny;
+        ray_grid(args[i], &nx, &ny);
+        cost[i] = (double)nx * ny * std::max(args[i].params.steps_min, args[i].params.steps_max);
+        int j = i;
+        while (j > 0 && cost[order[j - 1]] < cost[i]) {
+            order[j] = order[j - 1];
+            --j;
+        }
+        order[j] = i;
+    }
+    const int tw = ctx->batch_tile_w, th = ctx->batch_tile_h;
+    long long n_tiles = 0;
+    for (int o = 0; o < n_views; ++o) {
+        int nx, ny;
+        ray_grid(args[order[o]], &nx, &ny);
+        n_tiles += (long long)((nx + tw - 1) / tw) * ((ny + th - 1) / th);
+    }
+    if (n_tiles > MT_NOALLOC_MAX_TILES)
+        return fail(ctx, MT_ERR_INVALID_ARG,
+                    "the batch needs %lld tiles of %dx%d rays; the fixed tile list holds %d", n_tiles, tw, th,
+                    MT_NOALLOC_MAX_TILES);
+    long long t = 0;
+    for (int o = 0; o < n_views; ++o) {
+        const int i = order[o];
+        int nx, ny;
+        ray_grid(args[i], &nx, &ny);
+        for (int y = 0; y < ny; y += th)
+            for (int x = 0; x < nx; x += tw) tiles[t++] = mt::BatchTile{i, x, y, nx, ny};
+    }
+    // The work counter must start at zero: it is part of the first copy.
+    std::memset(g_noalloc_host, 0, kNoallocViewsOff);
+    cudaStream_t s = (cudaStream_t)stream;
+    MT_CUDA(ctx, cudaMemcpyAsync(dev, g_noalloc_host, kNoallocViewsOff + (size_t)n_views * sizeof(mt::MarchArgs),
+                                 cudaMemcpyHostToDevice, s));
+    if (n_tiles > 0)
+        MT_CUDA(ctx, cudaMemcpyAsync(dev + kNoallocTilesOff, tiles, (size_t)n_tiles * sizeof(mt::BatchTile),
+                                     cudaMemcpyHostToDevice, s));
+    for (int i = 0; i < n_views; ++i)
+        if (!(args[i].flags & MT_RENDER_FULL)) MT_CUDA(ctx, mt::launch_reproject(args[i], s));
+    if (n_tiles == 0) return MT_OK;
+    mt::BatchArgs b;
+    b.views = reinterpret_cast<const mt::MarchArgs*>(dev + kNoallocViewsOff);
+    b.tiles = reinterpret_cast<const mt::BatchTile*>(dev + kNoallocTilesOff);
+    b.counter = reinterpret_cast<unsigned*>(dev);
+    b.stats = count ? ctx->stats : nullptr;
+    b.n_tiles = (int32_t)n_tiles;
+    b.tile_w = tw;
+    b.tile_h = th;
+    const int storage = views[0].params.storage;
+    const int lanes = ctx->batch_lanes;
+    const int blocks = storage == MT_STORAGE_F16    ? mt::batch_blocks_f16(ctx->device, lanes)
+                       : storage == MT_STORAGE_BF16 ? mt::batch_blocks_bf16(ctx->device, lanes)
+                                                    : mt::batch_blocks_u8(ctx->device, lanes);
+    MT_CUDA(ctx, storage == MT_STORAGE_F16    ? mt::launch_batch_f16(b, lanes, blocks, s)
+                 : storage == MT_STORAGE_BF16 ? mt::launch_batch_bf16(b, lanes, blocks, s)
+                                              : mt::launch_batch_u8(b, lanes, blocks, s));
     return MT_OK;
 }
 
