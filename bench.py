@@ -51,6 +51,9 @@ def parse():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the batched (config 3), precision (config 2) and serving (config 4) legs")
+    ap.add_argument("--serve-requests", type=int, default=10000)
     return ap.parse_args()
 
 
@@ -176,6 +179,187 @@ def run_reference(args) -> int:
 
 
 # ---------------------------------------------------------------------------
+# forms beside the headline: batched, precision, serving (GPU, rank 0 only)
+# ---------------------------------------------------------------------------
+def _timed_reps(torch, flush, fn, reps):
+    """Mean ms of fn() over `reps` runs, each after an L2 flush, device events."""
+    stream = torch.cuda.current_stream()
+    out = []
+    for r in range(reps):
+        flush.fill_(float(r))
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        b.synchronize()
+        out.append(a.elapsed_time(b))
+    return statistics.mean(out)
+
+
+def bench_batched(ctx, torch, flush, reps: int = 3) -> dict:
+    """Config 3: 64 views of uneven resolution, full raymarch, step budgets
+    U{64..128}, per-view weather maps (seed + view id), one persistent
+    graph-captured launch; RGBA8 (FP32 math) and FP16 storage, against one
+    mt_render per view."""
+    from meteoros_gb300 import abi, scenes
+
+    specs = scenes.config3_views(SEED, n_views=64)
+    for v in range(64):
+        ctx.generate_weather(v, SEED + v)
+    imgs = [(torch.empty((h, w, 4), dtype=torch.float32, device="cuda"),
+             torch.empty((h, w), dtype=torch.float32, device="cuda")) for w, h, *_ in specs]
+    out = {"views": 64, "pixels": int(sum(w * h for w, h, *_ in specs))}
+    for name, storage in (("u8_fp32", abi.MT_STORAGE_U8), ("fp16", abi.MT_STORAGE_F16)):
+        views = []
+        for (w, h, cam, tm, params), (cur, mask) in zip(specs, imgs):
+            p = scenes.C_copy(abi.Params(), params)
+            p.storage = storage
+            p.fp64_shells = 0 if storage == abi.MT_STORAGE_U8 else 1
+            views.append(scenes.make_view(cam, cam, tm, p, cur, None, mask, abi.MT_RENDER_FULL))
+        best = ctx.autotune_batch(views)
+        counted = [scenes.make_view(v.camera, v.camera, v.time, v.params, c, None, m,
+                                    abi.MT_RENDER_FULL | abi.MT_RENDER_COUNT) for v, (c, m) in zip(views, imgs)]
+        ctx.stats(reset=True)
+        ctx.render_batch(counted)
+        samples = ctx.stats(reset=True).primary_samples
+        ms = _timed_reps(torch, flush, lambda: ctx.render_batch(views), reps)
+        out[name] = {"ms": round(ms, 3), "gsamples_per_s": round(samples / (ms * 1e-3) / 1e9, 3),
+                     "primary_samples": int(samples),
+                     "tile": [best.batch_tile_w, best.batch_tile_h], "lanes": best.batch_lanes}
+        if storage == abi.MT_STORAGE_U8:
+            def per_view():
+                for v, (cur, mask) in zip(views, imgs):
+                    ctx.render(v.camera, v.camera, v.time, v.params, None, cur, mask, abi.MT_RENDER_FULL)
+            pms = _timed_reps(torch, flush, per_view, reps)
+            out["per_view_u8_fp32"] = {"ms": round(pms, 3),
+                                       "gsamples_per_s": round(samples / (pms * 1e-3) / 1e9, 3)}
+    ctx.set_tuning(batch_tile=(16, 8), batch_lanes=1)
+    return out
+
+
+def bench_precision(ctx, torch, flush, reps: int = 3, err_stride: int = 16) -> dict:
+    """Config 2: one 3840x2160 full frame per storage; error against the FP64
+    oracle on every err_stride-th row and column (test infrastructure, used
+    here only as the checker)."""
+    import numpy as np
+
+    from meteoros_gb300 import abi, scenes
+
+    W, H = 3840, 2160
+    cam, tm, params, _ = scenes.config_view(SEED + 2, W, H)
+    cur = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+    mask = torch.empty((H, W), dtype=torch.float32, device="cuda")
+    out = {"width": W, "height": H}
+    ref_vols = None
+    try:
+        from oracle import pyoracle
+
+        g = pyoracle.generate_volumes(SEED)
+        ref_vols = {"u8_fp32": pyoracle.Volumes(g["base"], g["detail"], g["curl"], g["weather"]),
+                    "fp16": pyoracle.volumes_16(g, "h16"), "bf16": pyoracle.volumes_16(g, "b16")}
+        ys, xs = np.mgrid[0:H:err_stride, 0:W:err_stride]
+        xy = np.stack([xs.ravel(), ys.ravel()], 1).astype(np.int32)
+    except Exception:
+        ref_vols = None
+    for name, storage in (("u8_fp32", abi.MT_STORAGE_U8), ("fp16", abi.MT_STORAGE_F16),
+                          ("bf16", abi.MT_STORAGE_BF16)):
+        p = scenes.C_copy(abi.Params(), params)
+        p.storage = storage
+        p.fp64_shells = 0 if storage == abi.MT_STORAGE_U8 else 1
+        ctx.stats(reset=True)
+        ctx.render(cam, cam, tm, p, None, cur, mask, abi.MT_RENDER_FULL | abi.MT_RENDER_COUNT)
+        samples = ctx.stats(reset=True).primary_samples
+        ms = _timed_reps(torch, flush, lambda: ctx.render(cam, cam, tm, p, None, cur, mask, abi.MT_RENDER_FULL),
+                         reps)
+        ent = {"ms": round(ms, 3), "gsamples_per_s": round(samples / (ms * 1e-3) / 1e9, 3)}
+        if ref_vols is not None:
+            ref, _ = pyoracle.march_pixels(ref_vols[name], cam, tm, p, W, H, xy, dtype=np.float64)
+            got = cur.cpu().numpy()[xy[:, 1], xy[:, 0], :3].astype(np.float64)
+            r = ref[:, :3]
+            d = np.abs(got - r).max(-1)
+            bright = np.abs(r).max(-1) > 4096.0  # the sun disk: held to relative error
+            dn = d[~bright]
+            rel = (d[bright] / np.abs(r[bright]).max(-1)) if bright.any() else np.zeros(1)
+            ent["err_vs_fp64"] = {"max_abs": float(dn.max()), "mean_abs": float(dn.mean()),
+                                  "p99_abs": float(np.percentile(dn, 99)),
+                                  "frac_le_2e-3": float((dn <= 2e-3).mean()),
+                                  "bright_pixels": int(bright.sum()), "bright_max_rel": float(rel.max()),
+                                  "pixels": int(d.size)}
+        out[name] = ent
+    return out
+
+
+def bench_serving(ctx, torch, n_requests: int, per_request: bool, rate: float | None = 2000.0,
+                  n_sessions: int = 256, use_graph: bool = False) -> dict:
+    """Config 4: open-loop Poisson stream (rate req/s) over n_sessions
+    sessions; each request is one reprojected frame (1/16 of the pixels
+    marched) of its session, whose resolution is drawn from {640x360: 50%,
+    1280x720: 35%, 1920x1080: 15%} and whose camera yaws 0.5 deg/frame from a
+    seeded start.  Each session's first two frames are warm-up (the first
+    marches every pixel).  Latency = completion (host callback behind the
+    batch) - submit.  rate None: every request submitted at once (the
+    loop's capacity)."""
+    import numpy as np
+
+    from meteoros_gb300 import abi, scenes
+    from meteoros_gb300.server import Server
+
+    rng = np.random.default_rng(SEED + 4)
+    res = [(640, 360), (1280, 720), (1920, 1080)]
+    sess_res = [res[int(i)] for i in rng.choice(3, size=n_sessions, p=[0.5, 0.35, 0.15])]
+    targets = rng.integers(0, n_sessions, n_requests)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n_requests)) if rate else np.zeros(n_requests)
+    starts, params = [], []
+    for i in range(n_sessions):
+        _, _, prm, (yaw, pitch) = scenes.config_view(SEED * 31 + i, *sess_res[i])
+        starts.append((yaw, pitch))
+        params.append(prm)
+
+    def frame(i, k):
+        w, h = sess_res[i]
+        yaw, pitch = starts[i]
+        cam = scenes.look((0.0, 100.0, 0.0), yaw + 0.5 * k, pitch, 60.0, w, h)
+        tm = abi.time_init()
+        tm.frame_count_mod16 = k % 16
+        tm.time[0] = 0.16 if k else 0.0
+        tm.time[1] = 0.16 * k
+        return cam, tm
+
+    count = [2] * n_sessions
+    reqs = []
+    for j in range(n_requests):
+        i = int(targets[j])
+        reqs.append((i, *frame(i, count[i])))
+        count[i] += 1
+    with Server(ctx, max_batch=64, streams=1 if per_request else 2, hbm_budget_bytes=40 << 30,
+                per_request=per_request, use_graph=use_graph) as srv:
+        sids = [srv.open_session(w, h, p) for (w, h), p in zip(sess_res, params)]
+        for k in range(2):
+            for r in [srv.submit(s, *frame(i, k)) for i, s in enumerate(sids)]:
+                srv.wait(r, 120000)
+        used, _ = srv.memory()
+        ctx.stats(reset=True)
+        t0 = time.perf_counter()
+        rids = []
+        for j, (i, cam, tm) in enumerate(reqs):
+            due = t0 + arrivals[j]
+            while time.perf_counter() < due:
+                pass
+            rids.append(srv.submit(sids[i], cam, tm))
+        late_s = time.perf_counter() - (t0 + arrivals[-1])
+        infos = [srv.wait(r, 120000) for r in rids]
+        samples = ctx.stats(reset=True).primary_samples
+    lat = np.array([x.done_s - x.submit_s for x in infos]) * 1e3
+    span = max(x.done_s for x in infos) - min(x.submit_s for x in infos)
+    return {"requests": n_requests, "sessions": n_sessions, "rate_req_s": rate or "all at once",
+            "p50_ms": round(float(np.percentile(lat, 50)), 3), "p99_ms": round(float(np.percentile(lat, 99)), 3),
+            "max_ms": round(float(lat.max()), 3), "mean_batch": round(float(np.mean([x.batch_size for x in infos])), 2),
+            "throughput_req_s": round(n_requests / span, 1),
+            "gsamples_per_s": round(samples / span / 1e9, 3), "primary_samples": int(samples),
+            "session_hbm_bytes": int(used), "submit_lag_s": round(late_s, 4)}
+
+
+# ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
 def run_gb300(args) -> int:
@@ -189,14 +373,14 @@ def run_gb300(args) -> int:
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
 
-    from meteoros_gb300 import abi, build, scenes
+    from meteoros_gb300 import abi, build, replicas, scenes
     from meteoros_gb300.renderer import Context, FrameInputs, Session
 
     build.build()
     ctx = Context(local)
     ctx.generate_volumes(SEED)
     total = args.warmup + args.steps
-    seq = scenes.config_sequence(SEED + rank, WIDTH, HEIGHT, frames=total)
+    seq = scenes.config_sequence(replicas.rank_seed(SEED, rank), WIDTH, HEIGHT, frames=total)
     frames = [FrameInputs(*f) for f in seq]
     sess = Session(ctx, WIDTH, HEIGHT, txaa=True)
     stream = torch.cuda.current_stream()
@@ -234,10 +418,7 @@ def run_gb300(args) -> int:
     ctx.set_timing(False)
     frame_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     ms = sum(frame_ms) / len(frame_ms)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = replicas.max_over_ranks(ms, dev)
 
     # ---- executed samples of the timed frames (counting pass, not timed) ----
     counter = Session(ctx, WIDTH, HEIGHT, txaa=False)
@@ -302,6 +483,22 @@ def run_gb300(args) -> int:
         except Exception as e:  # the baseline never decides the GPU number
             cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": f"failed: {e}"}
 
+    forms = None
+    if world == 1 and not args.no_forms:
+        forms = {}
+        n = args.serve_requests
+        for name, fn in (("batched_config3", lambda: bench_batched(ctx, torch, flush)),
+                         ("precision_config2", lambda: bench_precision(ctx, torch, flush)),
+                         ("serve_config4", lambda: bench_serving(ctx, torch, n, False)),
+                         ("serve_config4_graph", lambda: bench_serving(ctx, torch, n, False, use_graph=True)),
+                         ("serve_config4_per_request", lambda: bench_serving(ctx, torch, n, True)),
+                         ("serve_capacity", lambda: bench_serving(ctx, torch, n, False, rate=None)),
+                         ("serve_capacity_per_request", lambda: bench_serving(ctx, torch, n, True, rate=None))):
+            try:
+                forms[name] = fn()
+            except Exception as e:  # a form never decides the headline number
+                forms[name] = {"failed": f"{type(e).__name__}: {e}"}
+
     line = {
         "metric": METRIC, "value": round(ms, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": False, "scaling": "weak",
@@ -327,6 +524,7 @@ def run_gb300(args) -> int:
         "gpu_launches": 3 * args.steps,
         "wall_s_timed": round(wall, 3),
         "cpu_baseline": cpu,
+        "forms": forms,
     }
     print(json.dumps(line), flush=True)
     if world > 1:

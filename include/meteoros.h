@@ -161,7 +161,14 @@ typedef struct mt_tuning {
     int32_t batch_tile_w;  /* mt_render_batch: tile of rays a CTA takes at a time (default 16 x 8) */
     int32_t batch_tile_h;
     int32_t batch_lanes;   /* mt_render_batch: lanes per ray, 1, 4, 8 or 16 (default 1) */
-    int32_t _reserved[3];
+    int32_t batch_direct;  /* mt_render_batch: 0 = one CUDA graph per batch (default); 1 = the same
+                            * copies and launches issued directly on the stream (no capture
+                            * cost per batch: the serving loop's small batches) */
+    int32_t reproject_serial; /* mt_render / mt_render_frame, checkerboard: 0 = the reprojection
+                               * runs on a second stream beside the raymarch (default; the call
+                               * still completes in `stream` order); 1 = before it on `stream` */
+    int32_t march_block;   /* mt_render: raymarch CTA size, 32 or 128 threads; 0 = default (128) */
+    int32_t _reserved[4];
 } mt_tuning;
 
 /* One view of a batched render (config 3). */
@@ -302,6 +309,36 @@ MT_API mt_status mt_autotune_batch(mt_ctx* ctx, const mt_view* views, int n_view
 #define MT_NOALLOC_MAX_TILES 32768
 MT_API mt_status mt_render_batch_noalloc(mt_ctx* ctx, const mt_view* views, int n_views, void* stream);
 
+/* ---- Downstream passes (the consumers of the compute stage's outputs) ----
+ * Both are full-screen fragment passes in the reference: one fragment per
+ * pixel with in_uv at the pixel centre, storing with imageStore at
+ * pixelPos = clamp(round(dim * in_uv)), which is the fragment's own pixel or
+ * the next one (round half away from zero).  Where two fragments store to
+ * one pixel the later fragment in raster order wins; pixels no fragment
+ * stores to keep their input value (mt_godrays) or their previous contents
+ * (mt_tonemap's output).  Device pointers, stream-ordered. */
+
+/* postProcess_GodRays.frag:66-149: 100-sample screen-space radial blur of the
+ * god-ray mask toward the static sun at (0, 1, 0), added to the HDR image.
+ * `mask` is the R32F mask the raymarch writes (the decoded value the shader's
+ * extract32fFromRGBA8f reads; LINEAR filtering with exact FP32 weights,
+ * border = the decode of opaque black).  `light_color` is SunAndSky.lightColor
+ * (Sky.cpp:71: 1, 1, 0.57, 1).  out_rgba may equal in_rgba.  The pass is
+ * disabled in the reference's command buffer (Renderer.cpp:826-832). */
+MT_API mt_status mt_godrays(mt_ctx* ctx, const mt_camera_ubo* camera, const float light_color[4],
+                            const float* mask, const float* in_rgba, float* out_rgba, int width, int height,
+                            void* stream);
+
+/* postProcess_ToneMap.frag:68-84: Uncharted-2 filmic curve (exposure 2.5,
+ * white point 100, gamma 1/2.2) of the LINEAR-filtered HDR image
+ * (clamp-to-border opaque black) plus WangHash dither * 0.01 seeded with
+ * uint(time.y).  out_format MT_LDR_RGBA8: 4 bytes per pixel, UNORM
+ * (clamp to [0, 1], x255, round to nearest even, NaN -> 0; the shader's
+ * `rgba8` image); MT_LDR_RGBA32F: the float values the shader stores. */
+typedef enum mt_ldr_format { MT_LDR_RGBA8 = 0, MT_LDR_RGBA32F = 1 } mt_ldr_format;
+MT_API mt_status mt_tonemap(mt_ctx* ctx, const mt_time_ubo* time, const float* in_rgba, void* out, int width,
+                            int height, int out_format, void* stream);
+
 /* Counters accumulated by render calls made with MT_RENDER_COUNT since the
  * last reset.  Synchronises the stream. */
 MT_API mt_status mt_get_stats(mt_ctx* ctx, mt_stats* out, int reset, void* stream);
@@ -323,6 +360,64 @@ MT_API mt_status mt_selftest_division(mt_ctx* ctx, const float* a, const float* 
 MT_API mt_status mt_set_timing(mt_ctx* ctx, int enabled);
 /* Synchronises on the recorded events and returns their durations. */
 MT_API mt_status mt_get_kernel_times(mt_ctx* ctx, mt_kernel_times* out);
+
+/* ---- Serving (config 4): continuous batching of per-session frames ----
+ * No counterpart in the reference, whose one window renders one view per
+ * frame (main.cpp:172-194).  A server owns a worker thread that batches
+ * requests over the context's shared volumes; the context must not be used
+ * by anything else while the server exists.  A session keeps its two raw
+ * frames (the reprojection ping-pong, Renderer.cpp:131-136), its god-ray
+ * mask and its previous camera resident in HBM; sessions are admitted while
+ * width * height * 36 bytes each fit hbm_budget_bytes (else MT_ERR_BUDGET).
+ * Each request is one frame of one session: the first marches every pixel,
+ * later ones march one pixel per 4x4 block and reproject the previous frame.
+ * A batch takes every queued request whose session has no frame in flight
+ * (up to max_batch, in arrival order) into one mt_render_batch; with
+ * streams = 2 a batch formed while another runs overlaps it on the device.
+ * Results equal the same requests rendered one at a time. */
+typedef struct mt_server mt_server;
+
+typedef struct mt_server_config {
+    uint64_t hbm_budget_bytes;  /* admission limit for session state */
+    int32_t max_batch;          /* requests per batch, >= 1 */
+    int32_t streams;            /* batches in flight at once: 1 or 2 */
+    int32_t batch_lanes;        /* 0 = keep the context's tuning, else 1, 4, 8 or 16 */
+    int32_t per_request;        /* 1 = no batching: one mt_render per request (the plain
+                                   per-request launch the batched loop is compared with) */
+    int32_t use_graph;          /* 1 = each batch as a CUDA graph; 0 = direct launches (lower
+                                   host cost per batch) */
+    int32_t _reserved[1];
+} mt_server_config;
+
+typedef struct mt_request_info {
+    uint64_t id;
+    int64_t session;
+    double submit_s, start_s, done_s;  /* mt_server_clock() at submit, batch launch, completion */
+    int32_t batch_size;                /* requests in the batch that ran it */
+    int32_t status;                    /* mt_status of the request */
+} mt_request_info;
+
+/* Seconds on the monotonic clock the request times use. */
+MT_API double mt_server_clock(void);
+MT_API mt_status mt_server_create(mt_ctx* ctx, const mt_server_config* cfg, mt_server** out);
+/* Waits (at most 30 s) for the batches in flight, then frees every session. */
+MT_API void mt_server_destroy(mt_server* srv);
+MT_API const char* mt_server_last_error(const mt_server* srv);
+MT_API mt_status mt_server_open_session(mt_server* srv, int width, int height, const mt_params* params,
+                                        int64_t* session);
+/* Waits (at most 30 s, else MT_ERR_TIMEOUT) for the session's frame in flight. */
+MT_API mt_status mt_server_close_session(mt_server* srv, int64_t session);
+/* Queues one frame of `session`; the camera of the session's previous frame
+ * is its camera_old.  Host structures, copied before the call returns. */
+MT_API mt_status mt_server_submit(mt_server* srv, int64_t session, const mt_camera_ubo* camera,
+                                  const mt_time_ubo* time, uint64_t* request);
+/* Waits at most timeout_ms for the request (MT_ERR_TIMEOUT, request kept),
+ * fills `info` and forgets the request; returns the request's status. */
+MT_API mt_status mt_server_wait(mt_server* srv, uint64_t request, int timeout_ms, mt_request_info* info);
+/* Copies the session's last frame (RGBA32F) and mask (R32F) to host memory
+ * (either may be NULL); waits (at most 30 s) for its frame in flight. */
+MT_API mt_status mt_server_read_frame(mt_server* srv, int64_t session, float* host_rgba, float* host_mask);
+MT_API mt_status mt_server_memory(mt_server* srv, uint64_t* used_bytes, uint64_t* budget_bytes);
 
 #ifdef __cplusplus
 }

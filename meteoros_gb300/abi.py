@@ -21,6 +21,8 @@ MT_CURL_N = 128
 MT_WEATHER_N = 512
 MT_MAX_WEATHER_SLOTS = 256
 MT_NOALLOC_MAX_VIEWS = 64
+MT_LDR_RGBA8 = 0
+MT_LDR_RGBA32F = 1
 MT_NOALLOC_MAX_TILES = 32768
 
 MT_OK = 0
@@ -109,7 +111,8 @@ class Stats(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("march_lanes", C.c_int32), ("fused_resolve", C.c_int32), ("batch_tile_w", C.c_int32),
-                ("batch_tile_h", C.c_int32), ("batch_lanes", C.c_int32), ("_reserved", C.c_int32 * 3)]
+                ("batch_tile_h", C.c_int32), ("batch_lanes", C.c_int32), ("batch_direct", C.c_int32),
+                ("reproject_serial", C.c_int32), ("march_block", C.c_int32), ("_reserved", C.c_int32 * 4)]
 
 
 class KernelTimes(C.Structure):
@@ -131,6 +134,17 @@ class View(C.Structure):
         ("flags", C.c_uint32),
         ("_pad", C.c_int32),
     ]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_batch", C.c_int32), ("streams", C.c_int32),
+                ("batch_lanes", C.c_int32), ("per_request", C.c_int32), ("use_graph", C.c_int32),
+                ("_reserved", C.c_int32 * 1)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("id", C.c_uint64), ("session", C.c_int64), ("submit_s", C.c_double), ("start_s", C.c_double),
+                ("done_s", C.c_double), ("batch_size", C.c_int32), ("status", C.c_int32)]
 
 
 assert C.sizeof(CameraUBO) == 160
@@ -167,6 +181,19 @@ SIGNATURES = {
     "mt_get_stats": (C.c_int, [_P, C.POINTER(Stats), C.c_int, _P]),
     "mt_autotune_batch": (C.c_int, [_P, C.POINTER(View), C.c_int, _P, C.POINTER(Tuning)]),
     "mt_render_batch_noalloc": (C.c_int, [_P, C.POINTER(View), C.c_int, _P]),
+    "mt_godrays": (C.c_int, [_P, C.POINTER(CameraUBO), C.POINTER(C.c_float), _P, _P, _P, C.c_int, C.c_int, _P]),
+    "mt_tonemap": (C.c_int, [_P, C.POINTER(TimeUBO), _P, _P, C.c_int, C.c_int, C.c_int, _P]),
+    "mt_server_clock": (C.c_double, []),
+    "mt_server_create": (C.c_int, [_P, C.POINTER(ServerConfig), C.POINTER(_P)]),
+    "mt_server_destroy": (None, [_P]),
+    "mt_server_last_error": (C.c_char_p, [_P]),
+    "mt_server_open_session": (C.c_int, [_P, C.c_int, C.c_int, C.POINTER(Params), C.POINTER(C.c_int64)]),
+    "mt_server_close_session": (C.c_int, [_P, C.c_int64]),
+    "mt_server_submit": (C.c_int, [_P, C.c_int64, C.POINTER(CameraUBO), C.POINTER(TimeUBO),
+                                   C.POINTER(C.c_uint64)]),
+    "mt_server_wait": (C.c_int, [_P, C.c_uint64, C.c_int, C.POINTER(RequestInfo)]),
+    "mt_server_read_frame": (C.c_int, [_P, C.c_int64, _P, _P]),
+    "mt_server_memory": (C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "mt_set_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
     "mt_get_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
     "mt_selftest_division": (C.c_int, [_P, _P, _P, _P, _P, C.c_int, _P]),

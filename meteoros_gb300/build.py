@@ -39,11 +39,13 @@ FAST = ["--use_fast_math"]
 UNITS = {
     "mt_host.cpp": ["-x", "cu"],
     "mt_capi.cu": [],
+    "mt_server.cpp": ["-x", "cu"],
     "mt_render.cu": EXACT,
     "mt_march_u8.cu": EXACT,
     "mt_march_f16.cu": FAST,
     "mt_march_bf16.cu": FAST,
     "mt_noise.cu": EXACT,
+    "mt_post.cu": EXACT,
 }
 
 

@@ -38,9 +38,11 @@ struct mt_ctx {
     cudaEvent_t ev[8] = {};                   // reproject, march, txaa, resolve (start, end)
     bool ran[4] = {false, false, false, false};
     int march_lanes = 0;                      // step-parallel lanes per ray (mt_set_tuning); 0 = auto
+    int march_block = 128;                    // march_kernel CTA size (mt_set_tuning)
     int fused_resolve = 0;                    // mt_render_frame: reprojection fused with TXAA
     // mt_render_batch
     int batch_tile_w = 16, batch_tile_h = 8, batch_lanes = 1;
+    int batch_direct = 0;                     // 1: no graph, copies and launches issued on the stream
     // Two slots used in turn, so two batches may run at once on two streams.
     mt::MarchArgs* d_views[2] = {nullptr, nullptr};  // device view tables
     mt::BatchTile* d_tiles[2] = {nullptr, nullptr};  // device tile lists
@@ -53,6 +55,11 @@ struct mt_ctx {
     size_t cap_views = 0, cap_tiles = 0;
     cudaStream_t cap_stream = nullptr;        // private stream the batch graphs are captured on
     cudaGraphExec_t batch_exec[2] = {nullptr, nullptr};
+    // mt_render / mt_render_frame: the reprojection runs beside the raymarch
+    // on this stream (fork/join events); overlap = 0 keeps one stream
+    cudaStream_t aux = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+    int overlap = 1;
 };
 
 namespace {
@@ -199,6 +206,7 @@ mt_status build_march_args(mt_ctx* ctx, const mt_camera_ubo* cam, const mt_camer
     a->groups_x = mt::march_groups(w);
     a->groups_y = mt::march_groups(h);
     a->flags = flags;
+    a->block = ctx->march_block;
     a->lanes = ctx->march_lanes;
     if (a->lanes == 0) {
         // Auto: enough rays fill the GPU one lane per ray; fewer rays (a
@@ -210,6 +218,10 @@ mt_status build_march_args(mt_ctx* ctx, const mt_camera_ubo* cam, const mt_camer
 }
 
 }  // namespace
+
+namespace mt {
+int ctx_device(const mt_ctx* ctx) { return ctx->device; }
+}  // namespace mt
 
 extern "C" {
 
@@ -234,7 +246,10 @@ MT_API mt_status mt_create(mt_ctx** out, int device) {
     ctx->weather16[0].assign(MT_MAX_WEATHER_SLOTS, nullptr);
     ctx->weather16[1].assign(MT_MAX_WEATHER_SLOTS, nullptr);
     if (bind_device(ctx) != MT_OK || alloc(ctx, &ctx->stats, 4) != MT_OK ||
-        cudaMemset(ctx->stats, 0, 4 * sizeof(unsigned long long)) != cudaSuccess) {
+        cudaMemset(ctx->stats, 0, 4 * sizeof(unsigned long long)) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->join_ev, cudaEventDisableTiming) != cudaSuccess) {
         g_create_error = ctx->err.empty() ? "context set-up failed" : ctx->err;
         mt_destroy(ctx);
         return MT_ERR_CUDA;
@@ -270,6 +285,9 @@ MT_API void mt_destroy(mt_ctx* ctx) {
         if (ctx->batch_exec[k]) cudaGraphExecDestroy(ctx->batch_exec[k]);
     }
     if (ctx->cap_stream) cudaStreamDestroy(ctx->cap_stream);
+    if (ctx->aux) cudaStreamDestroy(ctx->aux);
+    if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
+    if (ctx->join_ev) cudaEventDestroy(ctx->join_ev);
     delete ctx;
 }
 
@@ -397,7 +415,8 @@ MT_API mt_status mt_render(mt_ctx* ctx, const mt_camera_ubo* camera, const mt_ca
     if (st != MT_OK) return st;
     if ((st = bind_device(ctx)) != MT_OK) return st;
     mt::LaunchEvents ev{{ctx->ev[0], ctx->ev[1]}, {ctx->ev[2], ctx->ev[3]}, {ctx->ev[6], ctx->ev[7]}, ctx->timing};
-    MT_CUDA(ctx, mt::launch_render(a, (cudaStream_t)stream, &ev));
+    const mt::ForkJoin fj{ctx->aux, ctx->fork_ev, ctx->join_ev};
+    MT_CUDA(ctx, mt::launch_render(a, (cudaStream_t)stream, &ev, ctx->overlap ? &fj : nullptr));
     if (ctx->timing) {
         ctx->ran[0] = !(flags & MT_RENDER_FULL) || ctx->ran[0];
         ctx->ran[1] = true;
@@ -426,7 +445,8 @@ MT_API mt_status mt_render_frame(mt_ctx* ctx, const mt_camera_ubo* camera, const
     a.fused_resolve = ctx->fused_resolve;
     if ((st = bind_device(ctx)) != MT_OK) return st;
     mt::LaunchEvents ev{{ctx->ev[0], ctx->ev[1]}, {ctx->ev[2], ctx->ev[3]}, {ctx->ev[6], ctx->ev[7]}, ctx->timing};
-    MT_CUDA(ctx, mt::launch_frame(a, (cudaStream_t)stream, &ev));
+    const mt::ForkJoin fj{ctx->aux, ctx->fork_ev, ctx->join_ev};
+    MT_CUDA(ctx, mt::launch_frame(a, (cudaStream_t)stream, &ev, ctx->overlap ? &fj : nullptr));
     if (ctx->timing) {
         ctx->ran[0] = ctx->ran[0] || (!(flags & MT_RENDER_FULL) && !ctx->fused_resolve);
         ctx->ran[1] = true;
@@ -463,6 +483,54 @@ MT_API mt_status mt_txaa(mt_ctx* ctx, const mt_camera_ubo* camera, const mt_came
     a.height = height;
     MT_CUDA(ctx, mt::launch_txaa(a, (cudaStream_t)stream, ctx->timing ? &ctx->ev[4] : nullptr));
     if (ctx->timing) ctx->ran[2] = true;
+    return MT_OK;
+}
+
+MT_API mt_status mt_godrays(mt_ctx* ctx, const mt_camera_ubo* camera, const float light_color[4], const float* mask,
+                            const float* in_rgba, float* out_rgba, int width, int height, void* stream) {
+    if (!ctx) return MT_ERR_INVALID_ARG;
+    if (!camera || !light_color) return fail(ctx, MT_ERR_INVALID_ARG, "camera and light_color must not be NULL");
+    mt_status st;
+    if ((st = check_image(ctx, width, height)) != MT_OK) return st;
+    if (!mask || !in_rgba || !out_rgba) return fail(ctx, MT_ERR_INVALID_ARG, "mask, in and out must not be NULL");
+    if (!aligned(in_rgba, 16) || !aligned(out_rgba, 16) || !aligned(mask, 4))
+        return fail(ctx, MT_ERR_INVALID_ARG, "images must be 16-byte aligned (mask 4-byte)");
+    if ((st = bind_device(ctx)) != MT_OK) return st;
+    mt::GodrayArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.camera = *camera;
+    for (int i = 0; i < 4; ++i) a.light[i] = light_color[i];
+    a.mask = mask;
+    a.in = (const float4*)in_rgba;
+    a.out = (float4*)out_rgba;
+    a.width = width;
+    a.height = height;
+    MT_CUDA(ctx, mt::launch_godrays(a, (cudaStream_t)stream));
+    return MT_OK;
+}
+
+MT_API mt_status mt_tonemap(mt_ctx* ctx, const mt_time_ubo* time, const float* in_rgba, void* out, int width,
+                            int height, int out_format, void* stream) {
+    if (!ctx) return MT_ERR_INVALID_ARG;
+    if (!time) return fail(ctx, MT_ERR_INVALID_ARG, "time must not be NULL");
+    mt_status st;
+    if ((st = check_image(ctx, width, height)) != MT_OK) return st;
+    if (out_format != MT_LDR_RGBA8 && out_format != MT_LDR_RGBA32F)
+        return fail(ctx, MT_ERR_INVALID_ARG, "out_format must be MT_LDR_RGBA8 or MT_LDR_RGBA32F");
+    if (!in_rgba || !out) return fail(ctx, MT_ERR_INVALID_ARG, "in and out must not be NULL");
+    if (!aligned(in_rgba, 16) || !aligned(out, out_format == MT_LDR_RGBA8 ? 4 : 16))
+        return fail(ctx, MT_ERR_INVALID_ARG, "in must be 16-byte aligned, out 4 (RGBA8) or 16 (RGBA32F)");
+    if ((const void*)in_rgba == out) return fail(ctx, MT_ERR_INVALID_ARG, "out must differ from in");
+    if ((st = bind_device(ctx)) != MT_OK) return st;
+    mt::TonemapArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.in = (const float4*)in_rgba;
+    a.out = out;
+    a.time_y = time->time[1];
+    a.format = out_format;
+    a.width = width;
+    a.height = height;
+    MT_CUDA(ctx, mt::launch_tonemap(a, (cudaStream_t)stream));
     return MT_OK;
 }
 
@@ -593,6 +661,27 @@ MT_API mt_status mt_render_batch(mt_ctx* ctx, const mt_view* views, int n_views,
                  : storage == MT_STORAGE_BF16 ? mt::batch_blocks_bf16(ctx->device, lanes)
                                               : mt::batch_blocks_u8(ctx->device, lanes);
 
+    if (ctx->batch_direct) {
+        // The same work as the graph below, issued on the caller's stream.
+        cudaStream_t s = (cudaStream_t)stream;
+        if (ctx->slot_pending[k]) MT_CUDA(ctx, cudaStreamWaitEvent(s, ctx->slot_done[k], 0));
+        MT_CUDA(ctx, cudaMemcpyAsync(ctx->d_views[k], h_views, args.size() * sizeof(mt::MarchArgs),
+                                     cudaMemcpyHostToDevice, s));
+        if (!tiles.empty())
+            MT_CUDA(ctx, cudaMemcpyAsync(ctx->d_tiles[k], h_tiles, tiles.size() * sizeof(mt::BatchTile),
+                                         cudaMemcpyHostToDevice, s));
+        MT_CUDA(ctx, cudaMemsetAsync(ctx->d_counter[k], 0, sizeof(unsigned), s));
+        for (int i = 0; i < n_views; ++i)
+            if (!(args[(size_t)i].flags & MT_RENDER_FULL)) MT_CUDA(ctx, mt::launch_reproject(args[(size_t)i], s));
+        if (!tiles.empty())
+            MT_CUDA(ctx, storage == MT_STORAGE_F16    ? mt::launch_batch_f16(b, lanes, blocks, s)
+                         : storage == MT_STORAGE_BF16 ? mt::launch_batch_bf16(b, lanes, blocks, s)
+                                                      : mt::launch_batch_u8(b, lanes, blocks, s));
+        MT_CUDA(ctx, cudaEventRecord(ctx->slot_done[k], s));
+        ctx->slot_pending[k] = true;
+        return MT_OK;
+    }
+
     cudaGraph_t graph = nullptr;
     cudaStream_t cs = ctx->cap_stream;
     MT_CUDA(ctx, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
@@ -713,11 +802,19 @@ MT_API mt_status mt_set_tuning(mt_ctx* ctx, const mt_tuning* t) {
         return fail(ctx, MT_ERR_INVALID_ARG, "batch tile must be 1..4096 rays");
     if (t->batch_lanes != 1 && t->batch_lanes != 4 && t->batch_lanes != 8 && t->batch_lanes != 16)
         return fail(ctx, MT_ERR_INVALID_ARG, "batch_lanes must be 1, 4, 8 or 16");
+    if (t->batch_direct != 0 && t->batch_direct != 1) return fail(ctx, MT_ERR_INVALID_ARG, "batch_direct must be 0 or 1");
+    if (t->reproject_serial != 0 && t->reproject_serial != 1)
+        return fail(ctx, MT_ERR_INVALID_ARG, "reproject_serial must be 0 or 1");
+    if (t->march_block != 0 && t->march_block != 32 && t->march_block != 128)
+        return fail(ctx, MT_ERR_INVALID_ARG, "march_block must be 0 (default 128), 32 or 128");
     ctx->march_lanes = t->march_lanes;
     ctx->fused_resolve = t->fused_resolve;
     ctx->batch_tile_w = t->batch_tile_w;
     ctx->batch_tile_h = t->batch_tile_h;
     ctx->batch_lanes = t->batch_lanes;
+    ctx->batch_direct = t->batch_direct;
+    ctx->overlap = t->reproject_serial ? 0 : 1;
+    ctx->march_block = t->march_block == 0 ? 128 : t->march_block;
     return MT_OK;
 }
 
@@ -730,6 +827,9 @@ MT_API mt_status mt_get_tuning(mt_ctx* ctx, mt_tuning* t) {
     t->batch_tile_w = ctx->batch_tile_w;
     t->batch_tile_h = ctx->batch_tile_h;
     t->batch_lanes = ctx->batch_lanes;
+    t->batch_direct = ctx->batch_direct;
+    t->reproject_serial = ctx->overlap ? 0 : 1;
+    t->march_block = ctx->march_block;
     return MT_OK;
 }
 

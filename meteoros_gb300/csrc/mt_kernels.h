@@ -27,6 +27,7 @@ struct MarchArgs {
     int32_t groups_x, groups_y;  // 4x4 blocks covered by the reference's raymarch dispatch
     uint32_t flags;
     int32_t lanes;               // lanes marching one ray together: 1, 4, 8 or 16
+    int32_t block;               // march_kernel CTA size: 32 or 128 threads
     const float4* history;       // mt_render_frame only: previous resolved frame
     float4* out;                 // mt_render_frame only: resolved frame
     int32_t fused_resolve;       // mt_render_frame: 1 = reprojection fused with TXAA
@@ -62,6 +63,25 @@ struct BatchArgs {
 };
 
 // Outputs of one generator launch (any pointer may be NULL).
+// postProcess_GodRays.frag over an HDR image (mt_godrays)
+struct GodrayArgs {
+    mt_camera_ubo camera;
+    float light[4];  // SunAndSky.lightColor
+    const float* mask;
+    const float4* in;
+    float4* out;  // may equal in
+    int32_t width, height;
+};
+
+// postProcess_ToneMap.frag (mt_tonemap)
+struct TonemapArgs {
+    const float4* in;
+    void* out;  // uint32 RGBA8 words or float4, by format
+    float time_y;
+    int32_t format;  // mt_ldr_format
+    int32_t width, height;
+};
+
 struct NoiseOut {
     uint32_t* u8;   // RGBA8 words
     uint2* h16;     // 4 x IEEE half per texel
@@ -76,7 +96,17 @@ struct LaunchEvents {
     bool on;
 };
 
-cudaError_t launch_render(const MarchArgs& a, cudaStream_t s, const LaunchEvents* ev);
+// A second stream for the reprojection of a checkerboard frame: it writes the
+// pixels the raymarch does not, so the two kernels may run at once (the
+// reprojection's blocks fill the SMs the raymarch's uneven rays leave idle).
+// fork is recorded on the caller's stream and waited on by aux; join the
+// other way.
+struct ForkJoin {
+    cudaStream_t aux;
+    cudaEvent_t fork, join;
+};
+
+cudaError_t launch_render(const MarchArgs& a, cudaStream_t s, const LaunchEvents* ev, const ForkJoin* fj);
 cudaError_t launch_reproject(const MarchArgs& a, cudaStream_t s);
 cudaError_t launch_march_u8(const MarchArgs& a, cudaStream_t s, long long rays);
 // Persistent batched march: `blocks` CTAs of 128 threads, `lanes` per ray.
@@ -90,8 +120,10 @@ int batch_blocks_bf16(int device, int lanes);
 cudaError_t launch_march_f16(const MarchArgs& a, cudaStream_t s, long long rays);
 cudaError_t launch_march_bf16(const MarchArgs& a, cudaStream_t s, long long rays);
 cudaError_t launch_txaa(const TxaaArgs& a, cudaStream_t s, const cudaEvent_t* ev);
+cudaError_t launch_godrays(const GodrayArgs& a, cudaStream_t s);
+cudaError_t launch_tonemap(const TonemapArgs& a, cudaStream_t s);
 // The raymarch, then reprojection fused with TXAA (a.history -> a.out).
-cudaError_t launch_frame(const MarchArgs& a, cudaStream_t s, const LaunchEvents* ev);
+cudaError_t launch_frame(const MarchArgs& a, cudaStream_t s, const LaunchEvents* ev, const ForkJoin* fj);
 cudaError_t launch_selftest_division(const float* a, const float* b, float* out_rdiv, float* out_ieee, int n,
                                      cudaStream_t s);
 cudaError_t launch_generate_base(uint32_t seed, NoiseOut o, cudaStream_t s);

@@ -305,9 +305,10 @@ MT_HD void march_pixel(const MarchArgs& a, const Frame& F, const Tex<S>& tx, int
 // Ray -> marched pixel.  Checkerboard: the reference's group grid covers
 // groups_x x groups_y blocks of 4x4 (Renderer.cpp:713-716); each ray is one
 // block's slot pixel.  Full: one ray per pixel.  G consecutive lanes (an
-// aligned segment of a warp) march one ray.
-template <int G, int S>
-__global__ void __launch_bounds__(128, 8) march_kernel(const __grid_constant__ MarchArgs a) {
+// aligned segment of a warp) march one ray.  BS threads per CTA (128 by
+// default, 32 selectable), 64 registers a thread either way.
+template <int G, int S, int BS>
+__global__ void __launch_bounds__(BS, 1024 / BS) march_kernel(const __grid_constant__ MarchArgs a) {
     static_assert(G >= 1 && G <= 32 && (32 % G) == 0, "G must divide the warp");
     const Frame F = make_frame(a.params);
     using T = typename Vol<S>::T;
@@ -348,20 +349,23 @@ __global__ void __launch_bounds__(128, 8) march_kernel(const __grid_constant__ M
 // marches its rays, 128/G rays per pass; per-view arguments come from the
 // view table in global memory.  Per-pixel results equal those of separate
 // march_kernel launches (the same march_pixel runs on the same inputs).
+//
+// Tiles are taken per warp, not per CTA: each warp runs its own loop, so a
+// warp that drew a cheap tile goes on to the next one while its neighbours
+// are still busy.
 template <int G, int S>
 __global__ void __launch_bounds__(128, 8) march_batch_kernel(const __grid_constant__ BatchArgs b) {
-    __shared__ int s_tile;
     using T = typename Vol<S>::T;
-    const int lane = (int)(threadIdx.x % G);
-    const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
-    constexpr int kRaysPerPass = 128 / G;
+    const int wl = (int)(threadIdx.x & 31);  // lane in the warp
+    const int lane = wl % G;
+    const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (wl & ~(G - 1)));
+    constexpr int kRaysPerPass = 32 / G;
     Counts cnt{0u, 0u, 0u};
     unsigned pixels = 0;
     for (;;) {
-        if (threadIdx.x == 0) s_tile = (int)atomicAdd(b.counter, 1u);
-        __syncthreads();
-        const int t = s_tile;
-        __syncthreads();
+        unsigned tt = 0;
+        if (wl == 0) tt = atomicAdd(b.counter, 1u);
+        const int t = (int)__shfl_sync(0xffffffffu, tt, 0);
         if (t >= b.n_tiles) break;
         const BatchTile tile = b.tiles[t];
         const MarchArgs& a = b.views[tile.view];
@@ -373,7 +377,7 @@ __global__ void __launch_bounds__(128, 8) march_batch_kernel(const __grid_consta
         const int step = full ? 1 : 4;
         const int tile_rays = b.tile_w * b.tile_h;
         for (int r0 = 0; r0 < tile_rays; r0 += kRaysPerPass) {
-            const int r = r0 + (int)(threadIdx.x / G);
+            const int r = r0 + wl / G;
             const int rx = tile.rx0 + r % b.tile_w, ry = tile.ry0 + r / b.tile_w;
             const int px = rx * step + sx, py = ry * step + sy;
             const bool active = r < tile_rays && rx < tile.nrx && ry < tile.nry && px < a.width && py < a.height;
@@ -408,15 +412,22 @@ template <int S> int batch_blocks_storage(int device, int lanes) {
     return (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
 }
 
-template <int S> cudaError_t launch_march_storage(const MarchArgs& a, cudaStream_t s, long long rays) {
+template <int S, int BS> void launch_march_bs(const MarchArgs& a, cudaStream_t s, long long rays) {
     const int G = a.lanes;
-    const unsigned blocks = (unsigned)((rays * G + 127) / 128);
+    const unsigned blocks = (unsigned)((rays * G + BS - 1) / BS);
     switch (G) {
-        case 1: march_kernel<1, S><<<blocks, 128, 0, s>>>(a); break;
-        case 4: march_kernel<4, S><<<blocks, 128, 0, s>>>(a); break;
-        case 16: march_kernel<16, S><<<blocks, 128, 0, s>>>(a); break;
-        default: march_kernel<8, S><<<blocks, 128, 0, s>>>(a); break;
+        case 1: march_kernel<1, S, BS><<<blocks, BS, 0, s>>>(a); break;
+        case 4: march_kernel<4, S, BS><<<blocks, BS, 0, s>>>(a); break;
+        case 16: march_kernel<16, S, BS><<<blocks, BS, 0, s>>>(a); break;
+        default: march_kernel<8, S, BS><<<blocks, BS, 0, s>>>(a); break;
     }
+}
+
+template <int S> cudaError_t launch_march_storage(const MarchArgs& a, cudaStream_t s, long long rays) {
+    if (a.block == 128)
+        launch_march_bs<S, 128>(a, s, rays);
+    else
+        launch_march_bs<S, 32>(a, s, rays);
     return cudaGetLastError();
 }
 

@@ -255,24 +255,38 @@ cudaError_t launch_reproject(const MarchArgs& a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_render(const MarchArgs& a, cudaStream_t s, const LaunchEvents* ev) {
+cudaError_t launch_render(const MarchArgs& a, cudaStream_t s, const LaunchEvents* ev, const ForkJoin* fj) {
     const bool timed = ev && ev->on;
-    if (!(a.flags & MT_RENDER_FULL)) {
+    if (a.flags & MT_RENDER_FULL) return launch_march(a, s, ev);
+    if (!fj) {
         if (timed) cudaEventRecord(ev->reproject[0], s);
         cudaError_t e = launch_reproject(a, s);
         if (timed) cudaEventRecord(ev->reproject[1], s);
         if (e != cudaSuccess) return e;
+        return launch_march(a, s, ev);
     }
-    return launch_march(a, s, ev);
+    // raymarch on s, reprojection beside it on aux (launched second, so the
+    // raymarch's blocks are dispatched first and the reprojection fills in)
+    cudaError_t e = cudaEventRecord(fj->fork, s);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(fj->aux, fj->fork, 0);
+    if (e != cudaSuccess) return e;
+    e = launch_march(a, s, ev);
+    if (e != cudaSuccess) return e;
+    if (timed) cudaEventRecord(ev->reproject[0], fj->aux);
+    e = launch_reproject(a, fj->aux);
+    if (timed) cudaEventRecord(ev->reproject[1], fj->aux);
+    if (e == cudaSuccess) e = cudaEventRecord(fj->join, fj->aux);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, fj->join, 0);
+    return e;
 }
 
 constexpr int kResolveTW = 32, kResolveTH = 8;
 
-cudaError_t launch_frame(const MarchArgs& a, cudaStream_t s, const LaunchEvents* ev) {
+cudaError_t launch_frame(const MarchArgs& a, cudaStream_t s, const LaunchEvents* ev, const ForkJoin* fj) {
     const bool timed = ev && ev->on;
     if (!a.fused_resolve) {
-        // reprojection, raymarch, TXAA as three launches
-        cudaError_t e = launch_render(a, s, ev);
+        // reprojection (beside the raymarch when fj is given), raymarch, TXAA
+        cudaError_t e = launch_render(a, s, ev, fj);
         if (e != cudaSuccess) return e;
         TxaaArgs t;
         t.camera = a.camera;

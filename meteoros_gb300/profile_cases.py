@@ -1,0 +1,108 @@
+"""Small, self-contained launches of each kernel, for profiling one kernel at a
+time under a profiler (a few launches, a few hundred MB on the device).
+
+  python -m meteoros_gb300.profile_cases <case> [--reps N]
+
+cases:
+  march_full      960x540 full-raymarch frame (march_kernel<1>), config 0 view
+  march_cb        1920x1080 checkerboard frame (march_kernel<4> + reprojection)
+  txaa            1920x1080 TXAA resolve
+  batch           64-view batched raymarch (march_batch_kernel), RGBA8 volumes
+  batch_fp16      the same with FP16 volumes
+  precision       3840x2160 full frame, FP16 volumes (march_kernel<1>, half2 path)
+  godrays         1920x1080 god-ray radial blur
+  tonemap         1920x1080 tone map + dither to RGBA8
+  generate        noise-volume generation (gen_* kernels)
+
+Each case renders its frame `reps` times (default 2) so a profiler can skip
+the first launch and capture the next.
+"""
+from __future__ import annotations
+
+import argparse
+import sys
+
+SEED = 2017
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("case")
+    ap.add_argument("--reps", type=int, default=2)
+    a = ap.parse_args(argv)
+
+    import torch
+
+    from . import abi, scenes
+    from .renderer import Context
+
+    ctx = Context(0)
+    ctx.generate_volumes(SEED)
+    dev = "cuda"
+    if a.case == "march_full":
+        cam, tm, params, _ = scenes.config_view(11, 960, 540)
+        cur = torch.zeros((540, 960, 4), device=dev)
+        for _ in range(a.reps):
+            ctx.render(cam, cam, tm, params, None, cur, None, abi.MT_RENDER_FULL)
+    elif a.case in ("march_cb", "txaa"):
+        W, H = 1920, 1080
+        cam, old, tm, params = scenes.config_sequence(SEED, W, H, frames=3)[2]
+        prev = torch.rand((H, W, 4), device=dev)
+        cur = torch.zeros_like(prev)
+        out = torch.zeros_like(prev)
+        for _ in range(a.reps):
+            if a.case == "march_cb":
+                ctx.render(cam, old, tm, params, prev, cur, None, abi.MT_RENDER_CHECKERBOARD)
+            else:
+                ctx.txaa(cam, old, tm, params, prev, cur, out)
+    elif a.case in ("batch", "batch_fp16"):
+        storage = abi.MT_STORAGE_F16 if a.case == "batch_fp16" else abi.MT_STORAGE_U8
+        specs = scenes.config3_views(SEED, n_views=64)
+        for v in range(64):
+            ctx.generate_weather(v, SEED + v)
+        views = []
+        keep = []
+        for w, h, cam, tm, params in specs:
+            params.storage = storage
+            params.fp64_shells = 0 if storage == abi.MT_STORAGE_U8 else 1
+            cur = torch.empty((h, w, 4), device=dev)
+            keep.append(cur)
+            views.append(scenes.make_view(cam, cam, tm, params, cur, None, None, abi.MT_RENDER_FULL))
+        for _ in range(a.reps):
+            ctx.render_batch(views)
+    elif a.case == "precision":
+        W, H = 3840, 2160
+        cam, tm, params, _ = scenes.config_view(SEED + 2, W, H)
+        params.storage = abi.MT_STORAGE_F16
+        params.fp64_shells = 1
+        cur = torch.empty((H, W, 4), device=dev)
+        for _ in range(a.reps):
+            ctx.render(cam, cam, tm, params, None, cur, None, abi.MT_RENDER_FULL)
+    elif a.case in ("godrays", "tonemap"):
+        W, H = 1920, 1080
+        img = torch.rand((H, W, 4), device=dev) * 2.0
+        mask = torch.rand((H, W), device=dev)
+        out = torch.empty_like(img)
+        out8 = torch.empty((H, W, 4), dtype=torch.uint8, device=dev)
+        cam = scenes.look((0.0, 0.0, 2.0), 5.0, 12.0, 45.0, W, H)
+        tm = abi.time_init()
+        tm.time[1] = 2.75
+        for _ in range(a.reps):
+            if a.case == "godrays":
+                ctx.godrays(cam, (1.0, 1.0, 0.57, 1.0), mask, img, out)
+            else:
+                ctx.tonemap(tm, img, out8, abi.MT_LDR_RGBA8)
+    elif a.case == "generate":
+        for r in range(a.reps):
+            ctx.generate_volumes(SEED + r)
+    else:
+        print(f"unknown case {a.case}", file=sys.stderr)
+        return 2
+    torch.cuda.synchronize()
+    ctx.close()
+    print("ok")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -127,6 +127,20 @@ class Context:
                                      C.byref(params), _ptr(current), _ptr(history), _ptr(out), w, h,
                                      _stream(stream)))
 
+    def godrays(self, camera, light_color, mask, inp, out, stream=None) -> None:
+        """God-ray radial blur of `mask` (H, W) added to `inp` (H, W, 4) into `out` (may be `inp`)."""
+        h, w = int(inp.shape[0]), int(inp.shape[1])
+        light = (C.c_float * 4)(*[float(x) for x in light_color])
+        self._check(self.lib.mt_godrays(self.handle, C.byref(camera), light, _ptr(mask), _ptr(inp), _ptr(out), w, h,
+                                        _stream(stream)))
+
+    def tonemap(self, time, inp, out, out_format: int = abi.MT_LDR_RGBA8, stream=None) -> None:
+        """Tone map + dither of `inp` (H, W, 4) into `out`: (H, W, 4) uint8 for
+        MT_LDR_RGBA8, (H, W, 4) float32 for MT_LDR_RGBA32F."""
+        h, w = int(inp.shape[0]), int(inp.shape[1])
+        self._check(self.lib.mt_tonemap(self.handle, C.byref(time), _ptr(inp), _ptr(out), w, h, int(out_format),
+                                        _stream(stream)))
+
     def render_batch(self, views: list[abi.View], stream=None) -> None:
         arr = (abi.View * len(views))(*views)
         self._check(self.lib.mt_render_batch(self.handle, arr, len(views), _stream(stream)))
@@ -138,7 +152,9 @@ class Context:
         return t
 
     def set_tuning(self, march_lanes: int | None = None, fused_resolve: bool | None = None,
-                   batch_tile: tuple[int, int] | None = None, batch_lanes: int | None = None) -> abi.Tuning:
+                   batch_tile: tuple[int, int] | None = None, batch_lanes: int | None = None,
+                   batch_direct: bool | None = None, reproject_serial: bool | None = None,
+                   march_block: int | None = None) -> abi.Tuning:
         t = abi.Tuning()
         self._check(self.lib.mt_get_tuning(self.handle, C.byref(t)))
         if march_lanes is not None:
@@ -149,6 +165,12 @@ class Context:
             t.batch_tile_w, t.batch_tile_h = batch_tile
         if batch_lanes is not None:
             t.batch_lanes = batch_lanes
+        if batch_direct is not None:
+            t.batch_direct = 1 if batch_direct else 0
+        if reproject_serial is not None:
+            t.reproject_serial = 1 if reproject_serial else 0
+        if march_block is not None:
+            t.march_block = march_block
         self._check(self.lib.mt_set_tuning(self.handle, C.byref(t)))
         return t
 

@@ -253,6 +253,7 @@ inline float exp(float x) { return std::exp(x); }
 inline vec3 exp(vec3 v) { return vec3(std::exp(v.x), std::exp(v.y), std::exp(v.z)); }
 inline float acos(float x) { return std::acos(x); }
 inline float cos(float x) { return std::cos(x); }
+inline float dot(vec2 a, vec2 b) { return a.x * b.x + a.y * b.y; }
 inline float dot(vec3 a, vec3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 inline float dot(vec4 a, vec4 b) { return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w; }
 inline float length(vec3 v) { return std::sqrt(dot(v, v)); }

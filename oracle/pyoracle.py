@@ -18,7 +18,7 @@ from meteoros_gb300 import abi
 ORACLE_DIR = Path(__file__).resolve().parent
 BUILD_DIR = ORACLE_DIR / "_build"
 LIB = BUILD_DIR / "liboracle.so"
-SOURCES = [ORACLE_DIR / "meteoros_oracle.cpp", ORACLE_DIR / "noise_oracle.cpp"]
+SOURCES = [ORACLE_DIR / "meteoros_oracle.cpp", ORACLE_DIR / "noise_oracle.cpp", ORACLE_DIR / "post_oracle.cpp"]
 HEADERS = [ORACLE_DIR / "oracle_math.hpp", ORACLE_DIR.parent / "include" / "meteoros.h"]
 
 CXXFLAGS = ["-O3", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-std=c++17"]
@@ -66,6 +66,12 @@ def lib() -> C.CDLL:
             f = getattr(L, name)
             f.restype = C.c_int
             f.argtypes = [C.POINTER(OrcVolumes), cam, tm, par, C.c_int, C.c_int, P, C.c_longlong, P, P, C.c_int]
+        L.orc_godrays_f32.restype = C.c_int
+        L.orc_godrays_f32.argtypes = [cam, P, P, P, P, C.c_int, C.c_int]
+        L.orc_tonemap_f32.restype = C.c_int
+        L.orc_tonemap_f32.argtypes = [C.c_float, P, P, P, C.c_int, C.c_int]
+        L.orc_wang_hash_noise.restype = C.c_float
+        L.orc_wang_hash_noise.argtypes = [C.c_uint32] * 3
         L.orc_generate_volumes.restype = None
         L.orc_generate_volumes.argtypes = [C.c_uint64] + [P] * 12
         L.orc_wang.restype = C.c_uint32
@@ -185,3 +191,27 @@ def txaa(cam, cam_old, tm, params, current, history, dtype=np.float32, nthreads:
     if rc != 0:
         raise RuntimeError(f"orc_txaa failed ({rc})")
     return out
+
+
+def godrays(cam, light_color, mask, rgba):
+    """God-ray radial blur added to (H, W, 4) `rgba` (restatement, FP32)."""
+    rgba = np.ascontiguousarray(rgba, np.float32)
+    mask = np.ascontiguousarray(mask, np.float32)
+    h, w = rgba.shape[:2]
+    out = np.empty_like(rgba)
+    light = np.ascontiguousarray(light_color, np.float32)
+    if lib().orc_godrays_f32(C.byref(cam), _ptr(light), _ptr(mask), _ptr(rgba), _ptr(out), w, h) != 0:
+        raise RuntimeError("orc_godrays_f32 failed")
+    return out
+
+
+def tonemap(time_y: float, rgba, fill4=np.nan, fill8=0):
+    """Tone map + dither.  Returns (float RGBA (H, W, 4), RGBA8 (H, W, 4) uint8);
+    pixels no fragment stores to keep the fill values."""
+    rgba = np.ascontiguousarray(rgba, np.float32)
+    h, w = rgba.shape[:2]
+    out4 = np.full((h, w, 4), fill4, np.float32)
+    out8 = np.full((h, w, 4), fill8, np.uint8)
+    if lib().orc_tonemap_f32(C.c_float(time_y), _ptr(rgba), _ptr(out4), _ptr(out8), w, h) != 0:
+        raise RuntimeError("orc_tonemap_f32 failed")
+    return out4, out8

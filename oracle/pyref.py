@@ -40,6 +40,10 @@ def lib() -> C.CDLL:
         L.ref_reprojection.argtypes = [cam, cam, tm, P, P, C.c_int, C.c_int, C.c_int]
         L.ref_txaa.restype = C.c_int
         L.ref_txaa.argtypes = [cam, cam, tm, P, P, P, C.c_int, C.c_int, C.c_int]
+        L.ref_godrays.restype = C.c_int
+        L.ref_godrays.argtypes = [cam, P, P, P, P, C.c_int, C.c_int]
+        L.ref_tonemap.restype = C.c_int
+        L.ref_tonemap.argtypes = [tm, P, P, C.c_int, C.c_int]
         L.ref_wang_hash_noise.restype = C.c_float
         L.ref_wang_hash_noise.argtypes = [C.c_uint, C.c_uint, C.c_uint]
         _lib = L
@@ -87,3 +91,23 @@ def txaa(cam, cam_old, tm, current, history, nthreads=0):
 
 def wang_hash_noise(u: int, v: int, s: int) -> float:
     return lib().ref_wang_hash_noise(u, v, s)
+
+
+def godrays(cam, light_color, mask, rgba):
+    """postProcess_GodRays.frag over (H, W, 4) `rgba` with the (H, W) mask."""
+    rgba = np.ascontiguousarray(rgba, np.float32)
+    mask = np.ascontiguousarray(mask, np.float32)
+    h, w = rgba.shape[:2]
+    out = np.empty_like(rgba)
+    light = np.ascontiguousarray(light_color, np.float32)
+    lib().ref_godrays(C.byref(cam), _p(light), _p(mask), _p(rgba), _p(out), w, h)
+    return out
+
+
+def tonemap(tm, rgba, fill=np.nan):
+    """postProcess_ToneMap.frag: the float values stored, `fill` where no fragment stores."""
+    rgba = np.ascontiguousarray(rgba, np.float32)
+    h, w = rgba.shape[:2]
+    out = np.full((h, w, 4), fill, np.float32)
+    lib().ref_tonemap(C.byref(tm), _p(rgba), _p(out), w, h)
+    return out

@@ -70,9 +70,11 @@ def transform(src: str) -> str:
     s = re.sub(r"layout\s*\([^)]*\)\s*uniform\s+(?:(?:writeonly|readonly)\s+)*(image2D|sampler2D|sampler3D)\s+(\w+)\s*;",
                r"\1 \2;", s)
     s = re.sub(r"layout\s*\([^)]*\)\s*(?:in|out)\s+(\w+)\s+(\w+)\s*;", r"thread_local \1 \2;", s)
-    s = re.sub(r"\binout\s+(\w+)\s+(\w+)", r"\1& \2", s)
-    s = re.sub(r"\bout\s+(\w+)\s+(\w+)", r"\1& \2", s)
-    s = re.sub(r"\bin\s+(\w+)\s+(\w+)", r"\1 \2", s)
+    # parameter qualifiers: on one line only (a comment's "in this" followed
+    # by a line break must stay a comment)
+    s = re.sub(r"\binout[ \t]+(\w+)[ \t]+(\w+)", r"\1& \2", s)
+    s = re.sub(r"\bout[ \t]+(\w+)[ \t]+(\w+)", r"\1& \2", s)
+    s = re.sub(r"\bin[ \t]+(\w+)[ \t]+(\w+)", r"\1 \2", s)
     s = _FLOAT.sub(lambda m: m.group(1) + "f", s)
     s = re.sub(r"(?<=[\w\)\]])\.([xyzw]{2,4}|[rgba]{2,4})\b(?=(\s*(?:\+=|-=|\*=|/=|=(?!=)))?)", _swizzle, s)
     s = re.sub(r"(?<=[\w\)\]])\.([rgba])\b(?!\w)", lambda m: "." + "xyzw"[_SWZ[m.group(1)]], s)

@@ -29,6 +29,9 @@ namespace sh_txaa {
 namespace sh_tonemap {
 #include "tonemap.inc"
 }  // namespace sh_tonemap
+namespace sh_godrays {
+#include "godrays.inc"
+}  // namespace sh_godrays
 }  // namespace glsl
 
 namespace {
@@ -165,6 +168,53 @@ __attribute__((visibility("default"))) int ref_txaa(const mt_camera_ubo* cam, co
             o[1] = S::outColor.y;
             o[2] = S::outColor.z;
             o[3] = S::outColor.w;
+        }
+    return 0;
+}
+
+// postProcess_GodRays.frag, one fragment per pixel in raster order with in_uv
+// at the pixel centre.  The mask is the sampler's image as texels
+// (mask, 0, 0, 0), which the shader's decode turns back into the mask value;
+// imageLoad reads in_rgba, imageStore writes out_rgba (first filled with
+// in_rgba), so where two fragments store to one pixel the later one wins.
+__attribute__((visibility("default"))) int ref_godrays(const mt_camera_ubo* cam, const float* light_color,
+                                                       const float* mask, const float* in_rgba, float* out_rgba,
+                                                       int width, int height) {
+    namespace S = glsl::sh_godrays;
+    const size_t n = (size_t)width * (size_t)height;
+    std::vector<float> texels(4 * n, 0.0f);
+    for (size_t i = 0; i < n; ++i) texels[4 * i] = mask[i];
+    for (size_t i = 0; i < 4 * n; ++i) out_rgba[i] = in_rgba[i];
+    set_tex(S::godRayCreationDataSampler, texels.data(), 1, width, height, 1, glsl::Address::ClampToBorder);
+    S::currentFrameResultImage = glsl::image2D{in_rgba, out_rgba, width, height};
+    load_camera(S::camera, cam);
+    S::sunAndSky.lightColor = v4(light_color);
+    for (int y = 0; y < height; ++y)
+        for (int x = 0; x < width; ++x) {
+            S::in_uv = glsl::vec2(((float)x + 0.5f) / (float)width, ((float)y + 0.5f) / (float)height);
+            S::shader_main();
+        }
+    return 0;
+}
+
+// postProcess_ToneMap.frag, one fragment per pixel in raster order.  The
+// shader's rgba8 image is kept as floats here (the values it stores);
+// out_rgba is left as the caller filled it where no fragment stores.
+__attribute__((visibility("default"))) int ref_tonemap(const mt_time_ubo* tm, const float* in_rgba, float* out_rgba,
+                                                       int width, int height) {
+    namespace S = glsl::sh_tonemap;
+    set_tex(S::inputImageSampler, in_rgba, 1, width, height, 1, glsl::Address::ClampToBorder);
+    S::currentFrameResultImage = glsl::image2D{nullptr, out_rgba, width, height};
+    S::haltonSeq1 = v4(tm->halton_seq1);
+    S::haltonSeq2 = v4(tm->halton_seq2);
+    S::haltonSeq3 = v4(tm->halton_seq3);
+    S::haltonSeq4 = v4(tm->halton_seq4);
+    S::time = glsl::vec2(tm->time[0], tm->time[1]);
+    S::frameCountMod16 = tm->frame_count_mod16;
+    for (int y = 0; y < height; ++y)
+        for (int x = 0; x < width; ++x) {
+            S::in_uv = glsl::vec2(((float)x + 0.5f) / (float)width, ((float)y + 0.5f) / (float)height);
+            S::shader_main();
         }
     return 0;
 }

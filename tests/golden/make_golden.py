@@ -12,6 +12,12 @@ oracle/ref_build.py from the reference tree -- on seeded synthetic inputs:
                           (Renderer.cpp:713-716) never marches columns 128-129
   txaa_out                postProcess_TXAA.frag on seeded current/history images
   wang_uvs, wang_val      WangHashNoise (postProcess_ToneMap.frag:52-66)
+  godray_*                postProcess_GodRays.frag over frame 15 of the sequence
+                          with the god-ray mask every frame of the sequence left
+                          (each frame writes its marched pixels; the image keeps
+                          the rest), light colour (1, 1, 0.57, 1) (Sky.cpp:71)
+  tonemap_*               postProcess_ToneMap.frag over the god-ray output,
+                          time.y = 2.75 (NaN where no fragment stores)
   gen_sha256_*            SHA-256 of the seed-7 generator volumes (pins the
                           generator bit for bit across hosts)
   *_ubo                   the exact uniform-block bytes every golden was made
@@ -49,6 +55,7 @@ OUT = Path(__file__).resolve().parent / "golden.npz"
 SEQ_W, SEQ_H, SEQ_PITCH = 64, 36, 20.0
 QUIRK_W, QUIRK_H, QUIRK_FRAME = 130, 18, 5
 KEEP = (0, 7, 15)
+GODRAY_LIGHT = np.array([1.0, 1.0, 0.57, 1.0], np.float32)
 
 
 def sequence_inputs():
@@ -125,13 +132,22 @@ def main() -> int:
     vol = golden_volumes(v)
     out = {}
     prev = initial_prev()
+    mask_image = np.zeros((SEQ_H, SEQ_W), np.float32)
     for f, (cam, old, tm) in enumerate(sequence_inputs()):
         out[f"seq_ubo_f{f}"] = ubo_bytes(cam, old, tm)
         rgba, mask = pyref.frame(vol, cam, old, tm, prev, SEQ_W, SEQ_H)
         if f in KEEP:
             out[f"repro_f{f}"] = rgba
             out[f"mask_f{f}"] = mask
+        mask_image = np.where(np.isnan(mask), mask_image, mask).astype(np.float32)
         prev = rgba
+    out["godray_ubo"] = ubo_bytes(cam)
+    out["godray_mask"] = mask_image
+    out["godray_out"] = pyref.godrays(cam, GODRAY_LIGHT, mask_image, prev)
+    tm = abi.time_init()
+    tm.time[1] = 2.75
+    out["tonemap_ubo"] = ubo_bytes(tm)
+    out["tonemap_out"] = pyref.tonemap(tm, out["godray_out"])
     cam = scenes.look((0.0, 0.0, 2.0), 0.0, SEQ_PITCH, 45.0, QUIRK_W, QUIRK_H)
     tm = abi.time_init()
     tm.frame_count_mod16 = QUIRK_FRAME

@@ -57,8 +57,9 @@ def per_view(ctx, bufs):
 def test_batch_equals_per_view(ctx, storage):
     views, bufs = build_views(storage)
     want, st_want = per_view(ctx, bufs)
-    for tile, lanes in (((16, 8), 1), ((8, 8), 4), ((32, 8), 8)):
-        ctx.set_tuning(batch_tile=tile, batch_lanes=lanes)
+    for tile, lanes, direct in (((16, 8), 1, False), ((8, 8), 4, False), ((32, 8), 8, False),
+                                ((16, 8), 1, True), ((16, 16), 4, True)):
+        ctx.set_tuning(batch_tile=tile, batch_lanes=lanes, batch_direct=direct)
         for b in bufs:
             b[4].fill_(float("nan"))
             b[5].fill_(float("nan"))
@@ -69,7 +70,7 @@ def test_batch_equals_per_view(ctx, storage):
             assert_bits_equal(b[5].cpu().numpy(), wm, f"view {i} mask, tile {tile} lanes {lanes}")
         assert (st.primary_samples, st.light_samples, st.marched_rays, st.pixels) == (
             st_want.primary_samples, st_want.light_samples, st_want.marched_rays, st_want.pixels)
-    ctx.set_tuning(batch_tile=(16, 8), batch_lanes=1)
+    ctx.set_tuning(batch_tile=(16, 8), batch_lanes=1, batch_direct=False)
 
 
 def test_autotune_keeps_results(ctx):
@@ -100,9 +101,11 @@ def test_batch_rejects_mixed_storage_and_bad_views(ctx):
     ctx.render_batch([])
 
 
-def test_batches_overlap_on_two_streams(ctx):
+@pytest.mark.parametrize("direct", [False, True])
+def test_batches_overlap_on_two_streams(ctx, direct):
     """Three batches over disjoint images on two streams (the second overlaps
     the first on the device; the third reuses the first one's slot)."""
+    ctx.set_tuning(batch_direct=direct)
     views, bufs = build_views()
     want, _ = per_view(ctx, bufs)
     for b in bufs:
@@ -119,3 +122,4 @@ def test_batches_overlap_on_two_streams(ctx):
     for i, (b, (wc, wm)) in enumerate(zip(bufs, want)):
         assert_bits_equal(b[4].cpu().numpy(), wc, f"view {i} rgba (two streams)")
         assert_bits_equal(b[5].cpu().numpy(), wm, f"view {i} mask (two streams)")
+    ctx.set_tuning(batch_direct=False)

@@ -298,12 +298,15 @@ def test_fused_frame_equals_render_then_txaa(ctx, size):
         out_a = torch.zeros_like(cur_a)
         ctx.render(cam, cam_old, tm, params, prev, cur_a, None, flags)
         ctx.txaa(cam, cam_old, tm, params, cur_a, hist, out_a)
-        for fused in (False, True):
-            ctx.set_tuning(fused_resolve=fused)
+        for fused, serial in ((False, False), (True, False), (False, True)):
+            ctx.set_tuning(fused_resolve=fused, reproject_serial=serial)
             cur_b = torch.zeros_like(cur_a)
             out_b = torch.zeros_like(cur_a)
             ctx.render_frame(cam, cam_old, tm, params, prev, cur_b, hist, out_b, None, flags)
-            what = f"{w}x{h} frame {frame} fused={fused}"
+            what = f"{w}x{h} frame {frame} fused={fused} serial={serial}"
             assert_bits_equal(cur_b.cpu().numpy(), cur_a.cpu().numpy(), what + " raw")
             assert_bits_equal(out_b.cpu().numpy(), out_a.cpu().numpy(), what + " resolved")
-        ctx.set_tuning(fused_resolve=False)
+            cur_c = torch.zeros_like(cur_a)
+            ctx.render(cam, cam_old, tm, params, prev, cur_c, None, flags)
+            assert_bits_equal(cur_c.cpu().numpy(), cur_a.cpu().numpy(), what + " mt_render")
+        ctx.set_tuning(fused_resolve=False, reproject_serial=False)

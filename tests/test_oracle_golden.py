@@ -120,3 +120,63 @@ def test_txaa_matches_reference_source(oracle, pyref, lib):
         a = oracle.txaa(cam, old, tm, abi.params_reference(), cur, hist)
         b = pyref.txaa(cam, old, tm, cur, hist)
         assert_bit_exact(a, b, f"txaa slot {f}")
+
+
+# ---- downstream passes: god-ray radial blur and tone map ----
+
+def test_godrays_match_golden(oracle, golden, lib):
+    (cam,) = mg.ubos_from(golden["godray_ubo"], abi.CameraUBO)
+    out = oracle.godrays(cam, mg.GODRAY_LIGHT, golden["godray_mask"], golden["repro_f15"])
+    assert_bit_exact(out, golden["godray_out"], "god rays")
+    assert np.abs(out - golden["repro_f15"]).max() > 0.1  # the blur adds light
+
+
+def test_tonemap_matches_golden(oracle, golden, lib):
+    (tm,) = mg.ubos_from(golden["tonemap_ubo"], abi.TimeUBO)
+    out4, out8 = oracle.tonemap(tm.time[1], golden["godray_out"])
+    ref = golden["tonemap_out"]
+    assert np.array_equal(np.isnan(out4), np.isnan(ref)), "stored-pixel pattern differs"
+    # powf of the host's libm: equal where the goldens were made, within 2 ulp elsewhere
+    ok = ~np.isnan(ref)
+    np.testing.assert_allclose(out4[ok], ref[ok], rtol=3e-7, atol=0)
+    # the RGBA8 image is the UNORM conversion of the stored values
+    conv = np.rint(np.clip(np.nan_to_num(out4, nan=0.0), 0.0, 1.0) * np.float32(255.0)).astype(np.uint8)
+    stored = ~np.isnan(out4[..., 3])
+    assert np.array_equal(out8[stored], conv[stored])
+
+
+def test_godray_and_tonemap_fragment_mapping(oracle):
+    """pixelPos = clamp(round(dim * in_uv)): column and row 0 receive no store,
+    the last column and row receive two (the later fragment wins)."""
+    w, h = 33, 17
+    img = np.random.default_rng(5).random((h, w, 4), dtype=np.float32)
+    out4, _ = oracle.tonemap(0.0, img)
+    stored = ~np.isnan(out4[..., 3])
+    assert not stored[0, :].any() and not stored[:, 0].any()
+    assert stored[-1, -1]
+
+
+def test_godrays_match_reference_source(oracle, pyref, lib):
+    rng = np.random.default_rng(21)
+    w, h = 61, 35
+    img = rng.random((h, w, 4), dtype=np.float32) * 3.0
+    mask = rng.random((h, w), dtype=np.float32) * 1.25
+    light = np.array([1.0, 1.0, 0.57, 1.0], np.float32)
+    for yaw, pitch in ((0.0, 0.0), (30.0, 25.0), (-50.0, 60.0), (10.0, -40.0), (180.0, 10.0)):
+        cam = mg.scenes.look((0.0, 0.0, 2.0), yaw, pitch, 45.0, w, h)
+        a = oracle.godrays(cam, light, mask, img)
+        b = pyref.godrays(cam, light, mask, img)
+        assert_bit_exact(a, b, f"god rays yaw {yaw} pitch {pitch}")
+
+
+def test_tonemap_matches_reference_source(oracle, pyref, lib):
+    rng = np.random.default_rng(22)
+    w, h = 59, 37
+    img = (rng.random((h, w, 4), dtype=np.float32) * 20.0).astype(np.float32)
+    img[3, 4] = 0.0  # black: the curve's zero crossing
+    for t in (0.0, 1.5, 977.25):
+        tm = abi.time_init()
+        tm.time[1] = t
+        a, _ = oracle.tonemap(t, img)
+        b = pyref.tonemap(tm, img)
+        assert_bit_exact(a, b, f"tone map t={t}")
