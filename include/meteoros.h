@@ -225,6 +225,24 @@ MT_API float mt_halton(int index, int base);
 MT_API mt_status mt_upload_volumes(mt_ctx* ctx, const uint8_t* base_rgba8, const uint8_t* detail_rgba8,
                                    const uint8_t* curl_rgba8, const uint8_t* weather_rgba8);
 MT_API mt_status mt_upload_weather(mt_ctx* ctx, int slot, const uint8_t* weather_rgba8);
+
+/* A noise volume from its stack of TGA slices, decoded on the device, in place
+ * of Sky::CreateCloudResources' stb_image loads (Sky.cpp:25-45,
+ * ImageLoadingUtility.cpp:75-139).  files[z] / sizes[z]: the bytes of slice z
+ * (the reference's "<name>(z+1).tga"), in host memory; MT_BASE_N slices of
+ * MT_BASE_N^2 for MT_VOLUME_BASE, MT_DETAIL_N of MT_DETAIL_N^2 for
+ * MT_VOLUME_DETAIL.  Decoded as the reference's loader does: image types 2
+ * (raw) and 10 (run-length) with colour-map type 0, 24 or 32 bits per pixel
+ * (24-bit pixels get alpha 255), rows flipped to top-first unless the origin
+ * is top-left, bytes past the end of a file read as 0.  Other files are
+ * rejected with MT_ERR_INVALID_ARG, as is a slice above
+ * MT_TGA_MAX_SLICE_BYTES.  Returns when the volume (and its FP16/BF16
+ * copies) is ready. */
+#define MT_VOLUME_BASE 0
+#define MT_VOLUME_DETAIL 1
+#define MT_TGA_MAX_SLICE_BYTES 200000
+MT_API mt_status mt_decode_tga_volume(mt_ctx* ctx, int volume, const uint8_t* const* files, const size_t* sizes,
+                                      int n_slices, void* stream);
 /* Generate the four noise volumes on the GPU from `seed` (no reference
  * counterpart: the reference loads pre-baked assets).  Writes RGBA8 and the
  * FP16/BF16 precision-form copies.  Weather goes to slot 0. */

@@ -22,6 +22,9 @@ MT_WEATHER_N = 512
 MT_MAX_WEATHER_SLOTS = 256
 MT_NOALLOC_MAX_VIEWS = 64
 MT_LDR_RGBA8 = 0
+MT_VOLUME_BASE = 0
+MT_VOLUME_DETAIL = 1
+MT_TGA_MAX_SLICE_BYTES = 200000
 MT_LDR_RGBA32F = 1
 MT_NOALLOC_MAX_TILES = 32768
 
@@ -181,6 +184,7 @@ SIGNATURES = {
     "mt_get_stats": (C.c_int, [_P, C.POINTER(Stats), C.c_int, _P]),
     "mt_autotune_batch": (C.c_int, [_P, C.POINTER(View), C.c_int, _P, C.POINTER(Tuning)]),
     "mt_render_batch_noalloc": (C.c_int, [_P, C.POINTER(View), C.c_int, _P]),
+    "mt_decode_tga_volume": (C.c_int, [_P, C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_size_t), C.c_int, _P]),
     "mt_godrays": (C.c_int, [_P, C.POINTER(CameraUBO), C.POINTER(C.c_float), _P, _P, _P, C.c_int, C.c_int, _P]),
     "mt_tonemap": (C.c_int, [_P, C.POINTER(TimeUBO), _P, _P, C.c_int, C.c_int, C.c_int, _P]),
     "mt_server_clock": (C.c_double, []),

@@ -46,6 +46,7 @@ UNITS = {
     "mt_march_bf16.cu": FAST,
     "mt_noise.cu": EXACT,
     "mt_post.cu": EXACT,
+    "mt_assets.cu": [],
 }
 
 

@@ -324,6 +324,66 @@ MT_API mt_status mt_upload_volumes(mt_ctx* ctx, const uint8_t* base, const uint8
     return MT_OK;
 }
 
+MT_API mt_status mt_decode_tga_volume(mt_ctx* ctx, int volume, const uint8_t* const* files, const size_t* sizes,
+                                      int n_slices, void* stream) {
+    if (!ctx) return MT_ERR_INVALID_ARG;
+    if (volume != MT_VOLUME_BASE && volume != MT_VOLUME_DETAIL)
+        return fail(ctx, MT_ERR_INVALID_ARG, "volume must be MT_VOLUME_BASE or MT_VOLUME_DETAIL");
+    const int n = volume == MT_VOLUME_BASE ? MT_BASE_N : MT_DETAIL_N;
+    if (n_slices != n) return fail(ctx, MT_ERR_INVALID_ARG, "%d slices given, the volume has %d", n_slices, n);
+    if (!files || !sizes) return fail(ctx, MT_ERR_INVALID_ARG, "files and sizes must not be NULL");
+    std::vector<mt::TgaSlice> table((size_t)n);
+    size_t total = 0, max_size = 0;
+    for (int z = 0; z < n; ++z) {
+        const uint8_t* f = files[z];
+        const size_t sz = sizes[z];
+        if (!f || sz < 18) return fail(ctx, MT_ERR_INVALID_ARG, "slice %d: not a TGA file (%zu bytes)", z, sz);
+        if (sz > MT_TGA_MAX_SLICE_BYTES)
+            return fail(ctx, MT_ERR_INVALID_ARG, "slice %d: %zu bytes, above the %d-byte limit", z, sz,
+                        MT_TGA_MAX_SLICE_BYTES);
+        const int type = f[2], bpp = f[16], w = f[12] | (f[13] << 8), h = f[14] | (f[15] << 8);
+        if (f[1] != 0 || (type != 2 && type != 10) || (bpp != 24 && bpp != 32))
+            return fail(ctx, MT_ERR_INVALID_ARG,
+                        "slice %d: unsupported TGA (colour-map type %d, image type %d, %d bits per pixel)", z, f[1],
+                        type, bpp);
+        if (w != n || h != n)
+            return fail(ctx, MT_ERR_INVALID_ARG, "slice %d is %dx%d, the volume's slices are %dx%d", z, w, h, n, n);
+        table[(size_t)z] = mt::TgaSlice{(long long)total, (long long)sz};
+        total += sz;
+        max_size = std::max(max_size, sz);
+    }
+    mt_status st;
+    if ((st = bind_device(ctx)) != MT_OK) return st;
+    if ((st = ensure_volumes(ctx)) != MT_OK) return st;
+    std::vector<uint8_t> blob(total);
+    for (int z = 0; z < n; ++z) std::memcpy(blob.data() + table[(size_t)z].offset, files[z], sizes[z]);
+    unsigned char* d_blob = nullptr;
+    mt::TgaSlice* d_table = nullptr;
+    cudaStream_t s = (cudaStream_t)stream;
+    uint32_t* vol = volume == MT_VOLUME_BASE ? ctx->base : ctx->detail;
+    cudaError_t e = cudaMalloc((void**)&d_blob, total);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&d_table, table.size() * sizeof(mt::TgaSlice));
+    if (e == cudaSuccess) e = cudaMemcpy(d_blob, blob.data(), total, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(d_table, table.data(), table.size() * sizeof(mt::TgaSlice), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = mt::launch_tga_decode(d_blob, d_table, n, max_size, vol, n, n, s);
+    const size_t texels = (size_t)n * n * n;
+    if (e == cudaSuccess)
+        e = mt::launch_u8_to_16(vol, texels, volume == MT_VOLUME_BASE ? ctx->base16[0] : ctx->detail16[0],
+                                volume == MT_VOLUME_BASE ? ctx->base16[1] : ctx->detail16[1], s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(d_blob);
+    cudaFree(d_table);
+    if (e != cudaSuccess)
+        return fail(ctx, e == cudaErrorMemoryAllocation ? MT_ERR_OUT_OF_MEMORY : MT_ERR_CUDA, "TGA decode: %s",
+                    cudaGetErrorString(e));
+    if (volume == MT_VOLUME_BASE)
+        ctx->have_base = true;
+    else
+        ctx->have_detail = true;
+    return MT_OK;
+}
+
 MT_API mt_status mt_upload_weather(mt_ctx* ctx, int slot, const uint8_t* weather) {
     if (!ctx) return MT_ERR_INVALID_ARG;
     if (!weather) return fail(ctx, MT_ERR_INVALID_ARG, "weather must not be NULL");

@@ -82,6 +82,12 @@ struct TonemapArgs {
     int32_t width, height;
 };
 
+// One TGA file of a volume's slice stack, inside the concatenated upload.
+struct TgaSlice {
+    long long offset;
+    long long size;
+};
+
 struct NoiseOut {
     uint32_t* u8;   // RGBA8 words
     uint2* h16;     // 4 x IEEE half per texel
@@ -121,6 +127,8 @@ cudaError_t launch_march_f16(const MarchArgs& a, cudaStream_t s, long long rays)
 cudaError_t launch_march_bf16(const MarchArgs& a, cudaStream_t s, long long rays);
 cudaError_t launch_txaa(const TxaaArgs& a, cudaStream_t s, const cudaEvent_t* ev);
 cudaError_t launch_godrays(const GodrayArgs& a, cudaStream_t s);
+cudaError_t launch_tga_decode(const unsigned char* blob, const TgaSlice* slices, int n_slices, size_t max_size,
+                              uint32_t* vol, int W, int H, cudaStream_t s);
 cudaError_t launch_tonemap(const TonemapArgs& a, cudaStream_t s);
 // The raymarch, then reprojection fused with TXAA (a.history -> a.out).
 cudaError_t launch_frame(const MarchArgs& a, cudaStream_t s, const LaunchEvents* ev, const ForkJoin* fj);

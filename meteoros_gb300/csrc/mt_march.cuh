@@ -159,6 +159,10 @@ MT_HD StepOut eval_step(const mt_params& p, const Frame& F, const Tex<S>& tx, co
     sp = sp + rc.wind * rc.total_time;
     Weather wt = weather_at<S>(p, F, tx, pos, rc.ec);
     if (p.height_gradient) wt.hgrad = height_gradient(relH, wt.type);
+    // A zero height gradient or zero coverage makes the density 0 (or NaN
+    // when the coverage is 0), never > 0: the step is empty whatever the base
+    // volume holds, so its texture fetch is skipped (results unchanged).
+    if ((p.height_gradient && wt.hgrad == 0.0f) || wt.mul == 0.0f) return o;
     float baseDensity = sample_low_frequency<S>(p, tx, sp, relH, wt) * 0.380f;
     if (baseDensity > 0.0f) {
         const Erosion ero = make_erosion(erosion_modifier<S>(tx, sp, relH));
@@ -314,7 +318,7 @@ __global__ void __launch_bounds__(BS, 1024 / BS) march_kernel(const __grid_const
     using T = typename Vol<S>::T;
     const Tex<S> tx{(const T*)a.vol[0], (const T*)a.vol[1], (const T*)a.vol[2], (const T*)a.vol[3]};
     const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long idx = tid / G;
+    const unsigned idx = (unsigned)(tid / G);  // rays < 2^31 (images are at most 16384^2)
     const int lane = (int)(threadIdx.x % G);
     const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
     Counts cnt{0u, 0u, 0u};
@@ -322,17 +326,17 @@ __global__ void __launch_bounds__(BS, 1024 / BS) march_kernel(const __grid_const
     int px = 0, py = 0;
     bool active;
     if (a.flags & MT_RENDER_FULL) {
-        active = idx < (long long)a.width * a.height;
+        active = (long long)idx < (long long)a.width * a.height;
         if (active) {
-            px = (int)(idx % a.width);
-            py = (int)(idx / a.width);
+            px = (int)(idx % (unsigned)a.width);
+            py = (int)(idx / (unsigned)a.width);
         }
     } else {
-        active = idx < (long long)a.groups_x * a.groups_y;
+        active = (long long)idx < (long long)a.groups_x * a.groups_y;
         if (active) {
             const int id = a.time.frame_count_mod16;
-            px = (int)(idx % a.groups_x) * 4 + a.params.slot_x[id];
-            py = (int)(idx / a.groups_x) * 4 + a.params.slot_y[id];
+            px = (int)(idx % (unsigned)a.groups_x) * 4 + a.params.slot_x[id];
+            py = (int)(idx / (unsigned)a.groups_x) * 4 + a.params.slot_y[id];
             active = px < a.width && py < a.height;
         }
     }

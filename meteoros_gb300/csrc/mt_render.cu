@@ -29,31 +29,83 @@ MT_HD bool is_marched(const MarchArgs& a, int x, int y) {
     return dx >= 0 && dy >= 0 && (dx & 3) == 0 && (dy & 3) == 0 && (dx >> 2) < a.groups_x && (dy >> 2) < a.groups_y;
 }
 
-// The previous camera's uv of the inner-shell hit of a ray
-// (reprojection.comp:205-222, postProcess_TXAA.frag:230-247).
-MT_HD void old_uv(const mt_params& p, const Frame& F, const mt_camera_ubo& cam, const mt_camera_ubo& cam_old,
-                  const mt_time_ubo& tm, float sx, float sy, int W, int H, bool repro, float& old_u, float& old_v) {
-    f3 eyePos = p.eye_sign * ld3(cam.eye);
-    Ray ray = cast_ray(sx, sy, eyePos, cam, tm, tm.frame_count_mod16, W, H, repro);
-    f3 ec = eyePos;
-    ec.y = -F.R;
-    Isect in = ray_sphere(ray.origin, ray.direction, ec, F.Rin);
-    const float* ov = cam_old.view;
-    f3 q = in.point;
+// The uniform part of the reprojection / TXAA geometry (cast_ray's camera
+// basis and jitter, ray_sphere's shifted origin and C, the reciprocals of the
+// per-frame denominators).  One thread per CTA evaluates it into shared
+// memory with the same operations, in the same order, as the per-pixel code
+// it lifts out of the pixel loop, so every pixel's result is unchanged bit for
+// bit; the pixels save ~15 IEEE divisions and 3 square roots each.
+struct ViewConsts {
+    f3 eye, right, up, ref, ec, ro;
+    float jx, jy, tanx, tany, C, Rin;
+    Rcp r_w, r_h, r_tanx, r_tany;
+    float ov[16];  // the previous camera's view matrix
+};
+
+MT_HD void make_view_consts(ViewConsts& v, const mt_params& p, const Frame& F, const mt_camera_ubo& cam,
+                            const mt_camera_ubo& cam_old, const mt_time_ubo& tm, int W, int H, bool repro) {
+    v.eye = p.eye_sign * ld3(cam.eye);
+    const float* m = cam.view;
+    v.right = normalize3(f3{m[0], m[4], m[8]});
+    v.up = normalize3(f3{m[1], m[5], m[9]});
+    const f3 look = -normalize3(f3{m[2], m[6], m[10]});
+    jitter_offset(tm, tm.frame_count_mod16, (float)W, (float)H, repro, v.jx, v.jy);
+    v.tanx = cam.tan_fov_by_2[0];
+    v.tany = cam.tan_fov_by_2[1];
+    v.ref = v.eye + look;
+    v.ec = v.eye;
+    v.ec.y = -F.R;
+    v.Rin = F.Rin;
+    v.ro = (v.eye - v.ec) / F.Rin;  // ray_sphere: rO = (rO - c) / radius, the ray origin being the eye
+    v.C = dot3(v.ro, v.ro) - 1.0f;
+    v.r_w = make_rcp((float)W);
+    v.r_h = make_rcp((float)H);
+    v.r_tanx = make_rcp(v.tanx);
+    v.r_tany = make_rcp(v.tany);
+    for (int i = 0; i < 16; ++i) v.ov[i] = cam_old.view[i];
+}
+
+// The previous camera's uv of the inner-shell hit of the ray through screen
+// point (sx, sy) (reprojection.comp:205-222, postProcess_TXAA.frag:230-247):
+// cast_ray (cloudRayMarch.comp:194-226) and ray_sphere (:229-273) with the
+// uniform parts taken from `v`.
+MT_HD void old_uv(const ViewConsts& v, float sx, float sy, float& old_u, float& old_v) {
+    float nx = sx * 2.0f - 1.0f, ny = sy * 2.0f - 1.0f;
+    nx = nx + v.jx;
+    ny = ny + v.jy;
+    const f3 cam_x = (nx * v.tanx) * v.right;
+    const f3 cam_y = (ny * v.tany) * v.up;
+    const f3 pp = v.ref + cam_x + cam_y;
+    const f3 rD = normalize3_r(pp - v.eye);
+    f3 q{0.0f, 0.0f, 0.0f};
+    const float A = dot3(rD, rD);
+    const float B = 2.0f * dot3(rD, v.ro);
+    const float disc = B * B - 4.0f * A * v.C;
+    if (!(disc < 0.0f)) {
+        float t = (-B - sqrtf(disc)) / (2.0f * A);
+        if (t < 0.0f) t = (-B + sqrtf(disc)) / (2.0f * A);
+        if (t >= 0.0f) {
+            f3 pnt = v.ro + t * rD;
+            pnt = pnt * v.Rin;
+            q = pnt + v.ec;
+        }
+    }
+    const float* ov = v.ov;
     f3 od{ov[0] * q.x + ov[4] * q.y + ov[8] * q.z + ov[12] * 1.0f, ov[1] * q.x + ov[5] * q.y + ov[9] * q.z + ov[13] * 1.0f,
           ov[2] * q.x + ov[6] * q.y + ov[10] * q.z + ov[14] * 1.0f};
-    od = normalize3(od);
-    od = od / (-od.z);
-    old_u = (od.x / cam.tan_fov_by_2[0]) * 0.5f + 0.5f;
-    old_v = (od.y / cam.tan_fov_by_2[1]) * 0.5f + 0.5f;
+    od = normalize3_r(od);
+    const Rcp rz = make_rcp(-od.z);
+    od = f3{rdiv(od.x, rz), rdiv(od.y, rz), rdiv(od.z, rz)};
+    old_u = rdiv(od.x, v.r_tanx) * 0.5f + 0.5f;
+    old_v = rdiv(od.y, v.r_tany) * 0.5f + 0.5f;
 }
 
 // reprojection.comp:193-244 for pixel (x, y).
-MT_HD f4v reproject_pixel(const MarchArgs& a, const Frame& F, int x, int y) {
+MT_HD f4v reproject_pixel(const MarchArgs& a, const ViewConsts& v, int x, int y) {
     const int W = a.width, H = a.height;
-    const float ux = (float)x / (float)W, uy = (float)y / (float)H;
+    const float ux = rdiv((float)x, v.r_w), uy = rdiv((float)y, v.r_h);
     float old_u, old_v;
-    old_uv(a.params, F, a.camera, a.camera_old, a.time, ux, uy, W, H, true, old_u, old_v);
+    old_uv(v, ux, uy, old_u, old_v);
     const float mx = old_u - ux, my = old_v - uy;
     f4v blur{0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll
@@ -66,14 +118,15 @@ MT_HD f4v reproject_pixel(const MarchArgs& a, const Frame& F, int x, int y) {
         const float4 s = __ldg(a.prev + (size_t)iy * (size_t)W + (size_t)ix);
         blur = blur + f4v{s.x, s.y, s.z, s.w};
     }
-    return blur / 10.0f;
+    const Rcp r10 = MT_RCP(0.0f, 10.0f);
+    return f4v{rdiv(blur.x, r10), rdiv(blur.y, r10), rdiv(blur.z, r10), rdiv(blur.w, r10)};
 }
 
 // The centre pixel of fragment (x, y)'s neighbourhood: pixelPos of
 // postProcess_TXAA.frag:227 with in_uv at the fragment centre.
-MT_HD void txaa_centre(int x, int y, int W, int H, float& iux, float& iuy, int& ppx, int& ppy) {
-    iux = ((float)x + 0.5f) / (float)W;
-    iuy = ((float)y + 0.5f) / (float)H;
+MT_HD void txaa_centre(const ViewConsts& v, int x, int y, int W, int H, float& iux, float& iuy, int& ppx, int& ppy) {
+    iux = rdiv((float)x + 0.5f, v.r_w);
+    iuy = rdiv((float)y + 0.5f, v.r_h);
     ppx = imin(imax(f2i(roundf((float)W * iux)), 0), W - 1);
     ppy = imin(imax(f2i(roundf((float)H * iuy)), 0), H - 1);
 }
@@ -81,23 +134,25 @@ MT_HD void txaa_centre(int x, int y, int W, int H, float& iux, float& iuy, int& 
 // postProcess_TXAA.frag:223-269 for fragment (x, y); `load(i, j)` reads the
 // current frame (0 outside the image, as imageLoad does).
 template <class Load>
-MT_HD f4v txaa_pixel(const mt_params& p, const Frame& F, const mt_camera_ubo& cam, const mt_camera_ubo& cam_old,
-                     const mt_time_ubo& tm, const float4* __restrict__ history, int x, int y, int W, int H,
-                     Load load) {
+MT_HD f4v txaa_pixel(const mt_params& p, const ViewConsts& v, const float4* __restrict__ history, int x, int y, int W,
+                     int H, Load load) {
     float iux, iuy;
     int ppx, ppy;
-    txaa_centre(x, y, W, H, iux, iuy, ppx, ppy);
+    txaa_centre(v, x, y, W, H, iux, iuy, ppx, ppy);
     float old_u, old_v;
-    old_uv(p, F, cam, cam_old, tm, iux, iuy, W, H, false, old_u, old_v);
+    old_uv(v, iux, iuy, old_u, old_v);
     f4v ctl = load(ppx - 1, ppy - 1), ctc = load(ppx, ppy - 1), ctr = load(ppx + 1, ppy - 1);
     f4v cml = load(ppx - 1, ppy), cmc = load(ppx, ppy), cmr = load(ppx + 1, ppy);
     f4v cbl = load(ppx - 1, ppy + 1), cbc = load(ppx, ppy + 1), cbr = load(ppx + 1, ppy + 1);
     f4v cmin = min4(ctl, min4(ctc, min4(ctr, min4(cml, min4(cmc, min4(cmr, min4(cbl, min4(cbc, cbr))))))));
     f4v cmax = max4(ctl, max4(ctc, max4(ctr, max4(cml, max4(cmc, max4(cmr, max4(cbl, max4(cbc, cbr))))))));
-    f4v cavg = (ctl + ctc + ctr + cml + cmc + cmr + cbl + cbc + cbr) / 9.0f;
+    const f4v s9 = ctl + ctc + ctr + cml + cmc + cmr + cbl + cbc + cbr;
+    const Rcp r9 = MT_RCP(0.0f, 9.0f), r5 = MT_RCP(0.0f, 5.0f);
+    f4v cavg = f4v{rdiv(s9.x, r9), rdiv(s9.y, r9), rdiv(s9.z, r9), rdiv(s9.w, r9)};
     f4v cmin5 = min4(ctc, min4(cml, min4(cmc, min4(cmr, cbc))));
     f4v cmax5 = max4(ctc, max4(cml, max4(cmc, max4(cmr, cbc))));
-    f4v cavg5 = (ctc + cml + cmc + cmr + cbc) / 5.0f;
+    const f4v s5 = ctc + cml + cmc + cmr + cbc;
+    f4v cavg5 = f4v{rdiv(s5.x, r5), rdiv(s5.y, r5), rdiv(s5.z, r5), rdiv(s5.w, r5)};
     cmin = f4v{0.5f * (cmin.x + cmin5.x), 0.5f * (cmin.y + cmin5.y), 0.5f * (cmin.z + cmin5.z), 0.5f * (cmin.w + cmin5.w)};
     cmax = f4v{0.5f * (cmax.x + cmax5.x), 0.5f * (cmax.y + cmax5.y), 0.5f * (cmax.z + cmax5.z), 0.5f * (cmax.w + cmax5.w)};
     cavg = f4v{0.5f * (cavg.x + cavg5.x), 0.5f * (cavg.y + cavg5.y), 0.5f * (cavg.z + cavg5.z), 0.5f * (cavg.w + cavg5.w)};
@@ -111,7 +166,11 @@ MT_HD f4v txaa_pixel(const mt_params& p, const Frame& F, const mt_camera_ubo& ca
     f4v v_clip = prev - f4v{p_clip.x, p_clip.y, p_clip.z, pc.w};
     float vux = fabsf(v_clip.x / e_clip.x), vuy = fabsf(v_clip.y / e_clip.y), vuz = fabsf(v_clip.z / e_clip.z);
     float ma = gmax(vux, gmax(vuy, vuz));
-    if (ma > 1.0f) prev = f4v{p_clip.x, p_clip.y, p_clip.z, pc.w} + v_clip / ma;
+    if (ma > 1.0f) {
+        const Rcp rm = make_rcp(ma);
+        prev = f4v{p_clip.x, p_clip.y, p_clip.z, pc.w} +
+               f4v{rdiv(v_clip.x, rm), rdiv(v_clip.y, rm), rdiv(v_clip.z, rm), rdiv(v_clip.w, rm)};
+    }
     const f3 lw{0.2125f, 0.7154f, 0.0721f};
     float lum0 = dot3(f3{curr.x, curr.y, curr.z}, lw);
     float lum1 = dot3(f3{prev.x, prev.y, prev.z}, lw);
@@ -122,19 +181,17 @@ MT_HD f4v txaa_pixel(const mt_params& p, const Frame& F, const mt_camera_ubo& ca
 }
 
 // reprojection.comp:193-244 for every pixel the march does not write.
+// 2D grid of 32x8-pixel CTAs (no index division; neighbouring taps share L1).
 __global__ void __launch_bounds__(256) reproject_kernel(const __grid_constant__ MarchArgs a) {
-    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ ViewConsts s_v;
     const int W = a.width, H = a.height;
-    bool active = idx < (long long)W * H;
-    int x = 0, y = 0;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    if (tid == 0) make_view_consts(s_v, a.params, make_frame(a.params), a.camera, a.camera_old, a.time, W, H, true);
+    __syncthreads();
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    const bool active = x < W && y < H && !is_marched(a, x, y);
     if (active) {
-        x = (int)(idx % W);
-        y = (int)(idx / W);
-        active = !is_marched(a, x, y);
-    }
-    if (active) {
-        const Frame F = make_frame(a.params);
-        const f4v b = reproject_pixel(a, F, x, y);
+        const f4v b = reproject_pixel(a, s_v, x, y);
         a.cur[(size_t)y * (size_t)W + (size_t)x] = make_float4(b.x, b.y, b.z, b.w);
     }
     if (a.stats) {
@@ -145,17 +202,19 @@ __global__ void __launch_bounds__(256) reproject_kernel(const __grid_constant__ 
 
 // postProcess_TXAA.frag:223-269, one thread per output pixel (fragment).
 __global__ void __launch_bounds__(256) txaa_kernel(const __grid_constant__ TxaaArgs a) {
-    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ ViewConsts s_v;
     const int W = a.width, H = a.height;
-    if (idx >= (long long)W * H) return;
-    const int x = (int)(idx % W), y = (int)(idx / W);
-    const Frame F = make_frame(a.params);
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    if (tid == 0) make_view_consts(s_v, a.params, make_frame(a.params), a.camera, a.camera_old, a.time, W, H, false);
+    __syncthreads();
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= W || y >= H) return;
     auto load = [&](int i, int j) -> f4v {
         if (i < 0 || j < 0 || i >= W || j >= H) return f4v{0.0f, 0.0f, 0.0f, 0.0f};
         float4 s = __ldg(a.current + (size_t)j * (size_t)W + (size_t)i);
         return f4v{s.x, s.y, s.z, s.w};
     };
-    const f4v r = txaa_pixel(a.params, F, a.camera, a.camera_old, a.time, a.history, x, y, W, H, load);
+    const f4v r = txaa_pixel(a.params, s_v, a.history, x, y, W, H, load);
     a.out[(size_t)y * (size_t)W + (size_t)x] = make_float4(r.x, r.y, r.z, r.w);
 }
 
@@ -171,9 +230,15 @@ template <int TW, int TH>
 __global__ void __launch_bounds__(TW * TH) resolve_kernel(const __grid_constant__ MarchArgs a) {
     constexpr int SW = TW + 3, SH = TH + 3;
     __shared__ float4 tile[SH][SW];
+    __shared__ ViewConsts s_rv, s_tv;  // reprojection and TXAA geometry
     const int W = a.width, H = a.height;
     const int x0 = blockIdx.x * TW - 1, y0 = blockIdx.y * TH - 1;
-    const Frame F = make_frame(a.params);
+    if (threadIdx.x == 0) {
+        const Frame F = make_frame(a.params);
+        make_view_consts(s_rv, a.params, F, a.camera, a.camera_old, a.time, W, H, true);
+        make_view_consts(s_tv, a.params, F, a.camera, a.camera_old, a.time, W, H, false);
+    }
+    __syncthreads();
     const bool full = (a.flags & MT_RENDER_FULL) != 0;
     unsigned reprojected = 0;
     for (int i = threadIdx.x; i < SW * SH; i += TW * TH) {
@@ -186,7 +251,7 @@ __global__ void __launch_bounds__(TW * TH) resolve_kernel(const __grid_constant_
                 const float4 c = a.cur[o];
                 v = f4v{c.x, c.y, c.z, c.w};
             } else {
-                v = reproject_pixel(a, F, x, y);
+                v = reproject_pixel(a, s_rv, x, y);
                 const bool owned = sx >= 1 && sy >= 1 && sx <= TW && sy <= TH;
                 if (owned) {
                     a.cur[o] = make_float4(v.x, v.y, v.z, v.w);
@@ -205,7 +270,7 @@ __global__ void __launch_bounds__(TW * TH) resolve_kernel(const __grid_constant_
             const float4 s = tile[j - y0][i - x0];
             return f4v{s.x, s.y, s.z, s.w};
         };
-        const f4v r = txaa_pixel(a.params, F, a.camera, a.camera_old, a.time, a.history, x, y, W, H, load);
+        const f4v r = txaa_pixel(a.params, s_tv, a.history, x, y, W, H, load);
         a.out[(size_t)y * (size_t)W + (size_t)x] = make_float4(r.x, r.y, r.z, r.w);
     }
     if (a.stats) {
@@ -250,8 +315,8 @@ static cudaError_t launch_march(const MarchArgs& a, cudaStream_t s, const Launch
 }
 
 cudaError_t launch_reproject(const MarchArgs& a, cudaStream_t s) {
-    const long long n = (long long)a.width * a.height;
-    reproject_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a);
+    const dim3 block(32, 8), grid((unsigned)((a.width + 31) / 32), (unsigned)((a.height + 7) / 8));
+    reproject_kernel<<<grid, block, 0, s>>>(a);
     return cudaGetLastError();
 }
 
@@ -316,9 +381,9 @@ cudaError_t launch_selftest_division(const float* a, const float* b, float* out_
 }
 
 cudaError_t launch_txaa(const TxaaArgs& a, cudaStream_t s, const cudaEvent_t* ev) {
-    const long long n = (long long)a.width * a.height;
     if (ev) cudaEventRecord(ev[0], s);
-    txaa_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a);
+    const dim3 block(32, 8), grid((unsigned)((a.width + 31) / 32), (unsigned)((a.height + 7) / 8));
+    txaa_kernel<<<grid, block, 0, s>>>(a);
     if (ev) cudaEventRecord(ev[1], s);
     return cudaGetLastError();
 }

@@ -18,7 +18,8 @@ from meteoros_gb300 import abi
 ORACLE_DIR = Path(__file__).resolve().parent
 BUILD_DIR = ORACLE_DIR / "_build"
 LIB = BUILD_DIR / "liboracle.so"
-SOURCES = [ORACLE_DIR / "meteoros_oracle.cpp", ORACLE_DIR / "noise_oracle.cpp", ORACLE_DIR / "post_oracle.cpp"]
+SOURCES = [ORACLE_DIR / "meteoros_oracle.cpp", ORACLE_DIR / "noise_oracle.cpp", ORACLE_DIR / "post_oracle.cpp",
+           ORACLE_DIR / "asset_oracle.cpp"]
 HEADERS = [ORACLE_DIR / "oracle_math.hpp", ORACLE_DIR.parent / "include" / "meteoros.h"]
 
 CXXFLAGS = ["-O3", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-std=c++17"]
@@ -70,6 +71,8 @@ def lib() -> C.CDLL:
         L.orc_godrays_f32.argtypes = [cam, P, P, P, P, C.c_int, C.c_int]
         L.orc_tonemap_f32.restype = C.c_int
         L.orc_tonemap_f32.argtypes = [C.c_float, P, P, P, C.c_int, C.c_int]
+        L.orc_decode_tga.restype = C.c_int
+        L.orc_decode_tga.argtypes = [P, C.c_size_t, C.POINTER(C.c_int), C.POINTER(C.c_int), P]
         L.orc_wang_hash_noise.restype = C.c_float
         L.orc_wang_hash_noise.argtypes = [C.c_uint32] * 3
         L.orc_generate_volumes.restype = None
@@ -215,3 +218,14 @@ def tonemap(time_y: float, rgba, fill4=np.nan, fill8=0):
     if lib().orc_tonemap_f32(C.c_float(time_y), _ptr(rgba), _ptr(out4), _ptr(out8), w, h) != 0:
         raise RuntimeError("orc_tonemap_f32 failed")
     return out4, out8
+
+
+def decode_tga(data: bytes) -> np.ndarray:
+    """TGA file bytes -> (H, W, 4) uint8 RGBA, top row first (restatement)."""
+    buf = np.frombuffer(data, np.uint8)
+    w, h = C.c_int(), C.c_int()
+    if lib().orc_decode_tga(_ptr(buf), len(data), C.byref(w), C.byref(h), None) != 0:
+        raise ValueError("TGA outside the accepted subset")
+    out = np.zeros((h.value, w.value, 4), np.uint8)
+    lib().orc_decode_tga(_ptr(buf), len(data), C.byref(w), C.byref(h), _ptr(out))
+    return out

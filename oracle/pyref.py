@@ -111,3 +111,37 @@ def tonemap(tm, rgba, fill=np.nan):
     out = np.full((h, w, 4), fill, np.float32)
     lib().ref_tonemap(C.byref(tm), _p(rgba), _p(out), w, h)
     return out
+
+
+_stbi = None
+
+
+def stbi_available() -> bool:
+    try:
+        return ref_build.build_stbi() is not None
+    except Exception:
+        return False
+
+
+def stbi_load_rgba(data: bytes) -> np.ndarray | None:
+    """The reference's stb_image decode of a TGA file to (H, W, 4) RGBA8
+    (None when stb_image rejects it)."""
+    global _stbi
+    if _stbi is None:
+        path = ref_build.build_stbi()
+        if path is None:
+            raise RuntimeError("reference tree not present: stb_image cannot be built")
+        L = C.CDLL(str(path))
+        L.ref_stbi_load_rgba.restype = C.c_int
+        L.ref_stbi_load_rgba.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_void_p,
+                                         C.c_longlong]
+        _stbi = L
+    buf = np.frombuffer(data, np.uint8)
+    w, h = C.c_int(), C.c_int()
+    cap = 4 * (data[12] | data[13] << 8) * (data[14] | data[15] << 8) if len(data) >= 18 else 0
+    cap = max(cap, 4)
+    out = np.zeros(cap, np.uint8)
+    rc = _stbi.ref_stbi_load_rgba(_p(buf), len(data), C.byref(w), C.byref(h), _p(out), cap)
+    if rc != 0:
+        return None
+    return out[: w.value * h.value * 4].reshape(h.value, w.value, 4).copy()

@@ -114,12 +114,36 @@ def build(reference: Path = DEFAULT_REF, force: bool = False) -> Path | None:
     return LIB
 
 
+STBI_LIB = OUT / "libstbi_ref.so"
+STBI_HEADER = "external/stb_image.h"
+
+
+def build_stbi(reference: Path = DEFAULT_REF, force: bool = False) -> Path | None:
+    """Build oracle/_ref/libstbi_ref.so: the reference's vendored stb_image
+    (external/stb_image.h, included from the reference tree) behind
+    oracle/ref_stbi.c.  None when the reference is absent."""
+    header = reference / STBI_HEADER
+    if not header.exists():
+        return None
+    OUT.mkdir(parents=True, exist_ok=True)
+    inputs = [header, ORACLE / "ref_stbi.c", Path(__file__)]
+    newest = max(p.stat().st_mtime for p in inputs)
+    if not force and STBI_LIB.exists() and STBI_LIB.stat().st_mtime >= newest:
+        return STBI_LIB
+    tmp = STBI_LIB.with_suffix(f".so.{os.getpid()}")
+    cmd = ["gcc", "-O2", "-fPIC", "-shared", "-w", f"-I{header.parent}", str(ORACLE / "ref_stbi.c"), "-o", str(tmp)]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, STBI_LIB)
+    return STBI_LIB
+
+
 def main() -> int:
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--reference", type=Path, default=DEFAULT_REF)
     ap.add_argument("--force", action="store_true")
     a = ap.parse_args()
     lib = build(a.reference, a.force)
+    build_stbi(a.reference, a.force)
     if lib is None:
         print(f"reference shaders not found under {a.reference}; nothing built")
         return 1

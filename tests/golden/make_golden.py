@@ -18,6 +18,9 @@ oracle/ref_build.py from the reference tree -- on seeded synthetic inputs:
                           the rest), light colour (1, 1, 0.57, 1) (Sky.cpp:71)
   tonemap_*               postProcess_ToneMap.frag over the god-ray output,
                           time.y = 2.75 (NaN where no fragment stores)
+  tga_sha256_base/detail  SHA-256 of the shipped noise volumes as the reference's
+                          loader builds them (stb_image on each TGA slice, slice z
+                          from "<name>(z+1).tga", ImageLoadingUtility.cpp:75-139)
   gen_sha256_*            SHA-256 of the seed-7 generator volumes (pins the
                           generator bit for bit across hosts)
   *_ubo                   the exact uniform-block bytes every golden was made
@@ -123,6 +126,12 @@ def wang_inputs():
     return np.random.default_rng(2).integers(0, 2**32, size=(256, 3), dtype=np.uint64).astype(np.uint32)
 
 
+def mg_textures() -> Path:
+    from oracle import ref_build
+
+    return ref_build.DEFAULT_REF / "src/CloudScapes/textures/CloudTextures"
+
+
 def main() -> int:
     build.build()
     if not pyref.available():
@@ -160,6 +169,10 @@ def main() -> int:
     uvs = wang_inputs()
     out["wang_uvs"] = uvs
     out["wang_val"] = np.array([pyref.wang_hash_noise(int(a), int(b), int(c)) for a, b, c in uvs], np.float32)
+    tex = mg_textures()
+    for kind, n, key in (("LowFrequency", 128, "tga_sha256_base"), ("HighFrequency", 32, "tga_sha256_detail")):
+        vol = np.stack([pyref.stbi_load_rgba((tex / kind / f"{kind}({z + 1}).tga").read_bytes()) for z in range(n)])
+        out[key] = np.frombuffer(hashlib.sha256(vol.tobytes()).digest(), np.uint8)
     for k in ("base", "detail", "curl", "weather"):
         for suffix in ("", "_h16", "_b16"):
             out[f"gen_sha256_{k}{suffix}"] = np.frombuffer(
