@@ -41,6 +41,10 @@ SEED = 2017
 METRIC = "1080p ms/frame"
 UNIT = "ms/frame"
 FLUSH_BYTES = 256 << 20
+# FP32 operations of the raymarch per visited pixel, marching ray, primary
+# sample and light sample, as counted by oracle/count_flops.py on the config-0
+# and config-1 views (every +, -, *, /, sqrt, exp, pow, acos, cos counted once).
+FLOPS_PER_PIXEL, FLOPS_PER_RAY, FLOPS_PER_PRIMARY, FLOPS_PER_LIGHT = 132.6, 506.5, 307.8, 229.6
 
 
 def parse():
@@ -429,6 +433,7 @@ def run_gb300(args) -> int:
     st = ctx.stats(reset=True)
     samples_per_frame = st.primary_samples / args.steps
     light_per_frame = st.light_samples / args.steps
+    rays_per_frame = st.marched_rays / args.steps
 
     # ---- end to end through the public API: host output buffers ----
     out_host = torch.empty((HEIGHT, WIDTH, 4), dtype=torch.float32, pin_memory=True)
@@ -471,6 +476,14 @@ def run_gb300(args) -> int:
     march_bytes = marched_px * (16 + 4) + volume_bytes  # colour + mask writes, volumes once (L2 flushed)
     achieved = march_bytes / (march_ms * 1e-3) / 1e9
     frame_bytes = (WIDTH * HEIGHT * 16) * 5 + WIDTH * HEIGHT // 16 * 4 + volume_bytes
+    # Algorithmic FP32 operations of the raymarch: the op-counting oracle
+    # (oracle/count_flops.py) fits FLOPs = P*pixels + R*rays + S*primary + L*light
+    # samples; the GPU's exact counters supply the four counts.
+    march_flops = (FLOPS_PER_PIXEL * marched_px + FLOPS_PER_RAY * rays_per_frame +
+                   FLOPS_PER_PRIMARY * samples_per_frame + FLOPS_PER_LIGHT * light_per_frame)
+    props = torch.cuda.get_device_properties(dev)
+    sm_max = float(peaks.get("sm_max_mhz", 2070.0))
+    fp32_peak = props.multi_processor_count * 128 * sm_max * 1e6 / 1e12  # non-fused FP32 ops/s, in T
     gsps = samples_per_frame / (ms * 1e-3) / 1e9
 
     cpu = None
@@ -516,6 +529,12 @@ def run_gb300(args) -> int:
                      "peak_source": peak_src,
                      "note": "the raymarch is FP32/L1-texel bound, not HBM bound: its HBM bytes are the colour and "
                              "mask writes plus one read of the noise volumes"},
+        "roofline_fp32": {"bound": "fp32", "kernel": "march_kernel",
+                          "achieved": round(march_flops / (march_ms * 1e-3) / 1e12, 3), "peak": round(fp32_peak, 2),
+                          "unit": "TFLOP/s", "frac": round(march_flops / (march_ms * 1e-3) / 1e12 / fp32_peak, 4),
+                          "flops_per_launch": int(march_flops),
+                          "peak_source": "nominal: SMs x 128 FP32 lanes x max SM clock, one non-fused op per lane "
+                                         "per clock (the kernels are built without contraction)"},
         "frame_hbm": {"algorithmic_bytes": frame_bytes,
                       "achieved_gbs": round(frame_bytes / (ms * 1e-3) / 1e9, 2)},
         "clocks": clk,

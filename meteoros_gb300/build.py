@@ -47,6 +47,7 @@ UNITS = {
     "mt_noise.cu": EXACT,
     "mt_post.cu": EXACT,
     "mt_assets.cu": [],
+    "mt_consts.cpp": ["-x", "cu", "-Xcompiler", "-ffp-contract=off"],
 }
 
 

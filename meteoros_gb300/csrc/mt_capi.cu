@@ -207,6 +207,8 @@ mt_status build_march_args(mt_ctx* ctx, const mt_camera_ubo* cam, const mt_camer
     a->groups_y = mt::march_groups(h);
     a->flags = flags;
     a->block = ctx->march_block;
+    mt::make_view_consts(&a->vc_repro, *p, *cam, *cam_old, *tm, w, h, true);
+    mt::make_view_consts(&a->vc_txaa, *p, *cam, *cam_old, *tm, w, h, false);
     a->lanes = ctx->march_lanes;
     if (a->lanes == 0) {
         // Auto: enough rays fill the GPU one lane per ray; fewer rays (a
@@ -541,6 +543,7 @@ MT_API mt_status mt_txaa(mt_ctx* ctx, const mt_camera_ubo* camera, const mt_came
     a.out = (float4*)out_rgba;
     a.width = width;
     a.height = height;
+    mt::make_view_consts(&a.vc, *params, *camera, *camera_old, *time, width, height, false);
     MT_CUDA(ctx, mt::launch_txaa(a, (cudaStream_t)stream, ctx->timing ? &ctx->ev[4] : nullptr));
     if (ctx->timing) ctx->ran[2] = true;
     return MT_OK;

@@ -10,6 +10,23 @@
 
 namespace mt {
 
+// The uniform part of the reprojection / TXAA geometry of one frame: the
+// camera basis, ray origin and jitter of cast_ray (cloudRayMarch.comp:194-226),
+// the shifted origin and constant term of ray_sphere's quadratic (:229-273)
+// for the inner shell, the reciprocals of the per-frame denominators (width,
+// height, tan(fov/2)) and the previous camera's view matrix.  Computed on the
+// host (mt_consts.cpp) with the same IEEE FP32 operations in the same order as
+// the per-pixel code it stands for, so every pixel's result is unchanged.
+struct ViewConsts {
+    float eye[3], right[3], up[3], ref[3], ec[3], ro[3];
+    float jx, jy, tanx, tany, C, Rin;
+    float r_w[2], r_h[2], r_tanx[2], r_tany[2];  // {b, RN(1/b)}
+    float ov[16];
+};
+
+void make_view_consts(ViewConsts* v, const mt_params& p, const mt_camera_ubo& cam, const mt_camera_ubo& cam_old,
+                      const mt_time_ubo& tm, int W, int H, bool repro);
+
 struct MarchArgs {
     mt_camera_ubo camera;
     mt_camera_ubo camera_old;
@@ -31,6 +48,8 @@ struct MarchArgs {
     const float4* history;       // mt_render_frame only: previous resolved frame
     float4* out;                 // mt_render_frame only: resolved frame
     int32_t fused_resolve;       // mt_render_frame: 1 = reprojection fused with TXAA
+    ViewConsts vc_repro;         // reprojection geometry (reprojection.comp's jitter)
+    ViewConsts vc_txaa;          // TXAA geometry (cloudRayMarch.comp's jitter)
 };
 
 struct TxaaArgs {
@@ -42,6 +61,7 @@ struct TxaaArgs {
     const float4* history;
     float4* out;
     int32_t width, height;
+    ViewConsts vc;
 };
 
 // One tile of a batched render: a TW x TH rectangle of one view's ray grid.

@@ -353,23 +353,20 @@ __global__ void __launch_bounds__(BS, 1024 / BS) march_kernel(const __grid_const
 // marches its rays, 128/G rays per pass; per-view arguments come from the
 // view table in global memory.  Per-pixel results equal those of separate
 // march_kernel launches (the same march_pixel runs on the same inputs).
-//
-// Tiles are taken per warp, not per CTA: each warp runs its own loop, so a
-// warp that drew a cheap tile goes on to the next one while its neighbours
-// are still busy.
 template <int G, int S>
 __global__ void __launch_bounds__(128, 8) march_batch_kernel(const __grid_constant__ BatchArgs b) {
+    __shared__ int s_tile;
     using T = typename Vol<S>::T;
-    const int wl = (int)(threadIdx.x & 31);  // lane in the warp
-    const int lane = wl % G;
-    const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (wl & ~(G - 1)));
-    constexpr int kRaysPerPass = 32 / G;
+    const int lane = (int)(threadIdx.x % G);
+    const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
+    constexpr int kRaysPerPass = 128 / G;
     Counts cnt{0u, 0u, 0u};
     unsigned pixels = 0;
     for (;;) {
-        unsigned tt = 0;
-        if (wl == 0) tt = atomicAdd(b.counter, 1u);
-        const int t = (int)__shfl_sync(0xffffffffu, tt, 0);
+        if (threadIdx.x == 0) s_tile = (int)atomicAdd(b.counter, 1u);
+        __syncthreads();
+        const int t = s_tile;
+        __syncthreads();
         if (t >= b.n_tiles) break;
         const BatchTile tile = b.tiles[t];
         const MarchArgs& a = b.views[tile.view];
@@ -381,7 +378,7 @@ __global__ void __launch_bounds__(128, 8) march_batch_kernel(const __grid_consta
         const int step = full ? 1 : 4;
         const int tile_rays = b.tile_w * b.tile_h;
         for (int r0 = 0; r0 < tile_rays; r0 += kRaysPerPass) {
-            const int r = r0 + wl / G;
+            const int r = r0 + (int)(threadIdx.x / G);
             const int rx = tile.rx0 + r % b.tile_w, ry = tile.ry0 + r / b.tile_w;
             const int px = rx * step + sx, py = ry * step + sy;
             const bool active = r < tile_rays && rx < tile.nrx && ry < tile.nry && px < a.width && py < a.height;

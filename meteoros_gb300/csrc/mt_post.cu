@@ -53,6 +53,13 @@ MT_HD float mask_decode(const float* __restrict__ m, int W, int H, float sx, flo
     const float fu = floorf(u), fv = floorf(v);
     const float a = u - fu, b = v - fv;
     const int i0 = f2i(fu), j0 = f2i(fv);
+    if (i0 >= 0 && j0 >= 0 && i0 < W - 1 && j0 < H - 1) {
+        // all four texels inside: the border channel interpolates zeros
+        const float* r = m + (size_t)j0 * (size_t)W + (size_t)i0;
+        const float x = lerp1(lerp1(__ldg(r), __ldg(r + 1), a), lerp1(__ldg(r + W), __ldg(r + W + 1), a), b);
+        const float w = lerp1(lerp1(0.0f, 0.0f, a), lerp1(0.0f, 0.0f, a), b);
+        return ((x * 1.0f + 0.0f) + 0.0f) + w * bit_dec_w();
+    }
     const long long i1 = (long long)i0 + 1, j1 = (long long)j0 + 1;
     float val[4], brd[4];
     const long long ii[2] = {i0, i1}, jj[2] = {j0, j1};

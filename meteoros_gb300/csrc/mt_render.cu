@@ -29,65 +29,32 @@ MT_HD bool is_marched(const MarchArgs& a, int x, int y) {
     return dx >= 0 && dy >= 0 && (dx & 3) == 0 && (dy & 3) == 0 && (dx >> 2) < a.groups_x && (dy >> 2) < a.groups_y;
 }
 
-// The uniform part of the reprojection / TXAA geometry (cast_ray's camera
-// basis and jitter, ray_sphere's shifted origin and C, the reciprocals of the
-// per-frame denominators).  One thread per CTA evaluates it into shared
-// memory with the same operations, in the same order, as the per-pixel code
-// it lifts out of the pixel loop, so every pixel's result is unchanged bit for
-// bit; the pixels save ~15 IEEE divisions and 3 square roots each.
-struct ViewConsts {
-    f3 eye, right, up, ref, ec, ro;
-    float jx, jy, tanx, tany, C, Rin;
-    Rcp r_w, r_h, r_tanx, r_tany;
-    float ov[16];  // the previous camera's view matrix
-};
-
-MT_HD void make_view_consts(ViewConsts& v, const mt_params& p, const Frame& F, const mt_camera_ubo& cam,
-                            const mt_camera_ubo& cam_old, const mt_time_ubo& tm, int W, int H, bool repro) {
-    v.eye = p.eye_sign * ld3(cam.eye);
-    const float* m = cam.view;
-    v.right = normalize3(f3{m[0], m[4], m[8]});
-    v.up = normalize3(f3{m[1], m[5], m[9]});
-    const f3 look = -normalize3(f3{m[2], m[6], m[10]});
-    jitter_offset(tm, tm.frame_count_mod16, (float)W, (float)H, repro, v.jx, v.jy);
-    v.tanx = cam.tan_fov_by_2[0];
-    v.tany = cam.tan_fov_by_2[1];
-    v.ref = v.eye + look;
-    v.ec = v.eye;
-    v.ec.y = -F.R;
-    v.Rin = F.Rin;
-    v.ro = (v.eye - v.ec) / F.Rin;  // ray_sphere: rO = (rO - c) / radius, the ray origin being the eye
-    v.C = dot3(v.ro, v.ro) - 1.0f;
-    v.r_w = make_rcp((float)W);
-    v.r_h = make_rcp((float)H);
-    v.r_tanx = make_rcp(v.tanx);
-    v.r_tany = make_rcp(v.tany);
-    for (int i = 0; i < 16; ++i) v.ov[i] = cam_old.view[i];
-}
-
 // The previous camera's uv of the inner-shell hit of the ray through screen
 // point (sx, sy) (reprojection.comp:205-222, postProcess_TXAA.frag:230-247):
 // cast_ray (cloudRayMarch.comp:194-226) and ray_sphere (:229-273) with the
 // uniform parts taken from `v`.
+MT_HD Rcp rcp_of(const float r[2]) { return Rcp{r[0], r[1]}; }
+
 MT_HD void old_uv(const ViewConsts& v, float sx, float sy, float& old_u, float& old_v) {
     float nx = sx * 2.0f - 1.0f, ny = sy * 2.0f - 1.0f;
     nx = nx + v.jx;
     ny = ny + v.jy;
-    const f3 cam_x = (nx * v.tanx) * v.right;
-    const f3 cam_y = (ny * v.tany) * v.up;
-    const f3 pp = v.ref + cam_x + cam_y;
-    const f3 rD = normalize3_r(pp - v.eye);
+    const f3 cam_x = (nx * v.tanx) * ld3(v.right);
+    const f3 cam_y = (ny * v.tany) * ld3(v.up);
+    const f3 pp = ld3(v.ref) + cam_x + cam_y;
+    const f3 rD = normalize3_r(pp - ld3(v.eye));
+    const f3 ro = ld3(v.ro);
     f3 q{0.0f, 0.0f, 0.0f};
     const float A = dot3(rD, rD);
-    const float B = 2.0f * dot3(rD, v.ro);
+    const float B = 2.0f * dot3(rD, ro);
     const float disc = B * B - 4.0f * A * v.C;
     if (!(disc < 0.0f)) {
         float t = (-B - sqrtf(disc)) / (2.0f * A);
         if (t < 0.0f) t = (-B + sqrtf(disc)) / (2.0f * A);
         if (t >= 0.0f) {
-            f3 pnt = v.ro + t * rD;
+            f3 pnt = ro + t * rD;
             pnt = pnt * v.Rin;
-            q = pnt + v.ec;
+            q = pnt + ld3(v.ec);
         }
     }
     const float* ov = v.ov;
@@ -96,14 +63,14 @@ MT_HD void old_uv(const ViewConsts& v, float sx, float sy, float& old_u, float& 
     od = normalize3_r(od);
     const Rcp rz = make_rcp(-od.z);
     od = f3{rdiv(od.x, rz), rdiv(od.y, rz), rdiv(od.z, rz)};
-    old_u = rdiv(od.x, v.r_tanx) * 0.5f + 0.5f;
-    old_v = rdiv(od.y, v.r_tany) * 0.5f + 0.5f;
+    old_u = rdiv(od.x, rcp_of(v.r_tanx)) * 0.5f + 0.5f;
+    old_v = rdiv(od.y, rcp_of(v.r_tany)) * 0.5f + 0.5f;
 }
 
 // reprojection.comp:193-244 for pixel (x, y).
 MT_HD f4v reproject_pixel(const MarchArgs& a, const ViewConsts& v, int x, int y) {
     const int W = a.width, H = a.height;
-    const float ux = rdiv((float)x, v.r_w), uy = rdiv((float)y, v.r_h);
+    const float ux = rdiv((float)x, rcp_of(v.r_w)), uy = rdiv((float)y, rcp_of(v.r_h));
     float old_u, old_v;
     old_uv(v, ux, uy, old_u, old_v);
     const float mx = old_u - ux, my = old_v - uy;
@@ -125,8 +92,8 @@ MT_HD f4v reproject_pixel(const MarchArgs& a, const ViewConsts& v, int x, int y)
 // The centre pixel of fragment (x, y)'s neighbourhood: pixelPos of
 // postProcess_TXAA.frag:227 with in_uv at the fragment centre.
 MT_HD void txaa_centre(const ViewConsts& v, int x, int y, int W, int H, float& iux, float& iuy, int& ppx, int& ppy) {
-    iux = rdiv((float)x + 0.5f, v.r_w);
-    iuy = rdiv((float)y + 0.5f, v.r_h);
+    iux = rdiv((float)x + 0.5f, rcp_of(v.r_w));
+    iuy = rdiv((float)y + 0.5f, rcp_of(v.r_h));
     ppx = imin(imax(f2i(roundf((float)W * iux)), 0), W - 1);
     ppy = imin(imax(f2i(roundf((float)H * iuy)), 0), H - 1);
 }
@@ -183,15 +150,11 @@ MT_HD f4v txaa_pixel(const mt_params& p, const ViewConsts& v, const float4* __re
 // reprojection.comp:193-244 for every pixel the march does not write.
 // 2D grid of 32x8-pixel CTAs (no index division; neighbouring taps share L1).
 __global__ void __launch_bounds__(256) reproject_kernel(const __grid_constant__ MarchArgs a) {
-    __shared__ ViewConsts s_v;
     const int W = a.width, H = a.height;
-    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-    if (tid == 0) make_view_consts(s_v, a.params, make_frame(a.params), a.camera, a.camera_old, a.time, W, H, true);
-    __syncthreads();
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     const bool active = x < W && y < H && !is_marched(a, x, y);
     if (active) {
-        const f4v b = reproject_pixel(a, s_v, x, y);
+        const f4v b = reproject_pixel(a, a.vc_repro, x, y);
         a.cur[(size_t)y * (size_t)W + (size_t)x] = make_float4(b.x, b.y, b.z, b.w);
     }
     if (a.stats) {
@@ -201,20 +164,31 @@ __global__ void __launch_bounds__(256) reproject_kernel(const __grid_constant__ 
 }
 
 // postProcess_TXAA.frag:223-269, one thread per output pixel (fragment).
-__global__ void __launch_bounds__(256) txaa_kernel(const __grid_constant__ TxaaArgs a) {
-    __shared__ ViewConsts s_v;
+// A 32x8 CTA stages the current frame over its pixels plus the halo the
+// neighbourhoods reach (the centre is the fragment's pixel or the next one:
+// one column/row before, two after) in shared memory, zero outside the image
+// as imageLoad returns; the nine taps per pixel then read shared memory.
+constexpr int kTxaaTW = 32, kTxaaTH = 8;
+__global__ void __launch_bounds__(kTxaaTW * kTxaaTH) txaa_kernel(const __grid_constant__ TxaaArgs a) {
+    constexpr int SW = kTxaaTW + 3, SH = kTxaaTH + 3;
+    __shared__ float4 tile[SH][SW];
     const int W = a.width, H = a.height;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-    if (tid == 0) make_view_consts(s_v, a.params, make_frame(a.params), a.camera, a.camera_old, a.time, W, H, false);
+    const int x0 = blockIdx.x * kTxaaTW - 1, y0 = blockIdx.y * kTxaaTH - 1;
+    for (int i = tid; i < SW * SH; i += kTxaaTW * kTxaaTH) {
+        const int gx = x0 + i % SW, gy = y0 + i / SW;
+        tile[i / SW][i % SW] = (gx >= 0 && gy >= 0 && gx < W && gy < H)
+                                   ? __ldg(a.current + (size_t)gy * (size_t)W + (size_t)gx)
+                                   : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
     __syncthreads();
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int x = blockIdx.x * kTxaaTW + threadIdx.x, y = blockIdx.y * kTxaaTH + threadIdx.y;
     if (x >= W || y >= H) return;
     auto load = [&](int i, int j) -> f4v {
-        if (i < 0 || j < 0 || i >= W || j >= H) return f4v{0.0f, 0.0f, 0.0f, 0.0f};
-        float4 s = __ldg(a.current + (size_t)j * (size_t)W + (size_t)i);
+        const float4 s = tile[j - y0][i - x0];
         return f4v{s.x, s.y, s.z, s.w};
     };
-    const f4v r = txaa_pixel(a.params, s_v, a.history, x, y, W, H, load);
+    const f4v r = txaa_pixel(a.params, a.vc, a.history, x, y, W, H, load);
     a.out[(size_t)y * (size_t)W + (size_t)x] = make_float4(r.x, r.y, r.z, r.w);
 }
 
@@ -230,15 +204,8 @@ template <int TW, int TH>
 __global__ void __launch_bounds__(TW * TH) resolve_kernel(const __grid_constant__ MarchArgs a) {
     constexpr int SW = TW + 3, SH = TH + 3;
     __shared__ float4 tile[SH][SW];
-    __shared__ ViewConsts s_rv, s_tv;  // reprojection and TXAA geometry
     const int W = a.width, H = a.height;
     const int x0 = blockIdx.x * TW - 1, y0 = blockIdx.y * TH - 1;
-    if (threadIdx.x == 0) {
-        const Frame F = make_frame(a.params);
-        make_view_consts(s_rv, a.params, F, a.camera, a.camera_old, a.time, W, H, true);
-        make_view_consts(s_tv, a.params, F, a.camera, a.camera_old, a.time, W, H, false);
-    }
-    __syncthreads();
     const bool full = (a.flags & MT_RENDER_FULL) != 0;
     unsigned reprojected = 0;
     for (int i = threadIdx.x; i < SW * SH; i += TW * TH) {
@@ -251,7 +218,7 @@ __global__ void __launch_bounds__(TW * TH) resolve_kernel(const __grid_constant_
                 const float4 c = a.cur[o];
                 v = f4v{c.x, c.y, c.z, c.w};
             } else {
-                v = reproject_pixel(a, s_rv, x, y);
+                v = reproject_pixel(a, a.vc_repro, x, y);
                 const bool owned = sx >= 1 && sy >= 1 && sx <= TW && sy <= TH;
                 if (owned) {
                     a.cur[o] = make_float4(v.x, v.y, v.z, v.w);
@@ -270,7 +237,7 @@ __global__ void __launch_bounds__(TW * TH) resolve_kernel(const __grid_constant_
             const float4 s = tile[j - y0][i - x0];
             return f4v{s.x, s.y, s.z, s.w};
         };
-        const f4v r = txaa_pixel(a.params, s_tv, a.history, x, y, W, H, load);
+        const f4v r = txaa_pixel(a.params, a.vc_txaa, a.history, x, y, W, H, load);
         a.out[(size_t)y * (size_t)W + (size_t)x] = make_float4(r.x, r.y, r.z, r.w);
     }
     if (a.stats) {
@@ -363,6 +330,7 @@ cudaError_t launch_frame(const MarchArgs& a, cudaStream_t s, const LaunchEvents*
         t.out = a.out;
         t.width = a.width;
         t.height = a.height;
+        t.vc = a.vc_txaa;
         return launch_txaa(t, s, timed ? ev->resolve : nullptr);
     }
     cudaError_t e = launch_march(a, s, ev);
@@ -382,7 +350,8 @@ cudaError_t launch_selftest_division(const float* a, const float* b, float* out_
 
 cudaError_t launch_txaa(const TxaaArgs& a, cudaStream_t s, const cudaEvent_t* ev) {
     if (ev) cudaEventRecord(ev[0], s);
-    const dim3 block(32, 8), grid((unsigned)((a.width + 31) / 32), (unsigned)((a.height + 7) / 8));
+    const dim3 block(kTxaaTW, kTxaaTH),
+        grid((unsigned)((a.width + kTxaaTW - 1) / kTxaaTW), (unsigned)((a.height + kTxaaTH - 1) / kTxaaTH));
     txaa_kernel<<<grid, block, 0, s>>>(a);
     if (ev) cudaEventRecord(ev[1], s);
     return cudaGetLastError();
