@@ -45,6 +45,10 @@ FLUSH_BYTES = 256 << 20
 # sample and light sample, as counted by oracle/count_flops.py on the config-0
 # and config-1 views (every +, -, *, /, sqrt, exp, pow, acos, cos counted once).
 FLOPS_PER_PIXEL, FLOPS_PER_RAY, FLOPS_PER_PRIMARY, FLOPS_PER_LIGHT = 132.6, 506.5, 307.8, 229.6
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one march_kernel<4>
+# launch on this workload's 1080p checkerboard frame, from one ncu capture with
+# cold caches (the bench flushes L2 before every frame too).
+MARCH_DRAM_BYTES_PER_LAUNCH = 9106688 + 2998016
 
 
 def parse():
@@ -525,7 +529,8 @@ def run_gb300(args) -> int:
         "light_samples_per_frame": int(light_per_frame),
         "kernel_ms": {k: round(statistics.mean(v), 5) for k, v in kern.items()},
         "roofline": {"bound": "hbm", "kernel": "march_kernel", "achieved": round(achieved, 2),
-                     "peak": hbm_peak, "unit": "GB/s", "frac": round(achieved / hbm_peak, 5), "traffic": None,
+                     "peak": hbm_peak, "unit": "GB/s", "frac": round(achieved / hbm_peak, 5),
+                     "traffic": MARCH_DRAM_BYTES_PER_LAUNCH, "algorithmic_bytes": march_bytes,
                      "peak_source": peak_src,
                      "note": "the raymarch is FP32/L1-texel bound, not HBM bound: its HBM bytes are the colour and "
                              "mask writes plus one read of the noise volumes"},
