@@ -209,6 +209,7 @@ mt_status build_march_args(mt_ctx* ctx, const mt_camera_ubo* cam, const mt_camer
     a->block = ctx->march_block;
     mt::make_view_consts(&a->vc_repro, *p, *cam, *cam_old, *tm, w, h, true);
     mt::make_view_consts(&a->vc_txaa, *p, *cam, *cam_old, *tm, w, h, false);
+    mt::make_march_jitter(a->jitter, *tm);
     a->lanes = ctx->march_lanes;
     if (a->lanes == 0) {
         // Auto: enough rays fill the GPU one lane per ray; fewer rays (a

@@ -71,4 +71,16 @@ void make_view_consts(ViewConsts* v, const mt_params& p, const mt_camera_ubo& ca
     for (int i = 0; i < 16; ++i) v->ov[i] = cam_old.view[i];
 }
 
+void make_march_jitter(float out[16][3], const mt_time_ubo& tm) {
+    for (int index = 0; index < 16; ++index) {
+        float jx, jy;
+        jitter(tm, index, 1.0f, 1.0f, false, jx, jy);
+        jx = jx / 75.0f;
+        jy = jy / 75.0f;
+        out[index][0] = jx;
+        out[index][1] = (jx + jy) * 1.180f;
+        out[index][2] = jy;
+    }
+}
+
 }  // namespace mt

@@ -50,7 +50,13 @@ struct MarchArgs {
     int32_t fused_resolve;       // mt_render_frame: 1 = reprojection fused with TXAA
     ViewConsts vc_repro;         // reprojection geometry (reprojection.comp's jitter)
     ViewConsts vc_txaa;          // TXAA geometry (cloudRayMarch.comp's jitter)
+    // The raymarch's per-step jitter (cloudRayMarch.comp:629-633) for each of
+    // the 16 values of its index: jx = halton / 1 / 75, jy likewise, and
+    // (jx + jy) * 1.18, evaluated on the host in that order (make_march_jitter).
+    float jitter[16][3];
 };
+
+void make_march_jitter(float out[16][3], const mt_time_ubo& tm);
 
 struct TxaaArgs {
     mt_camera_ubo camera;

@@ -94,10 +94,11 @@ template <int S> MT_HD float erosion_modifier(const Tex<S>& tx, f3 point, float 
 struct RayConsts {
     Ray ray;
     f3 ec, startPos;
-    f3 kernel[6];
-    f3 wind, skew;
-    float stepSize, cos_angle, cos_q, HG_light, total_time;
+    f3 koff[6];  // cone-light offsets: (stepSize * kernel[i]) * i
+    f3 wind_t, skew;  // wind * total time
+    float stepSize, cos_angle, cos_q, HG_light, lenInner;
     int pixelID;
+    const float (*jitter)[3];  // per jitter index: (jx, (jx + jy) * 1.18, jy), see MarchArgs::jitter
 };
 
 static __device__ __noinline__ void ray_consts(const mt_params& p, const mt_time_ubo& tm, const Ray& ray, f3 ec,
@@ -121,15 +122,18 @@ static __device__ __noinline__ void ray_consts(const mt_params& p, const mt_time
         maxComp = f3{0.0f, 0.0f, az};
     f3 zC = cross3(lightDir, maxComp);
     f3 xC = cross3(zC, lightDir);
-    rc.kernel[0] = mat3mul(xC, lightDir, zC, f3{0.1f, 0.25f, -0.15f});
-    rc.kernel[1] = mat3mul(xC, lightDir, zC, f3{0.2f, 0.5f, 0.2f});
-    rc.kernel[2] = mat3mul(xC, lightDir, zC, f3{-0.2f, 0.1f, -0.1f});
-    rc.kernel[3] = mat3mul(xC, lightDir, zC, f3{-0.05f, 0.75f, 0.05f});
-    rc.kernel[4] = mat3mul(xC, lightDir, zC, f3{-0.1f, 1.0f, 0.0f});
-    rc.kernel[5] = mat3mul(xC, lightDir, zC, f3{0.0f, 3.0f, 0.0f});
-    rc.wind = ld3(p.wind_dir) * p.wind_speed;
+    const f3 kernel[6] = {mat3mul(xC, lightDir, zC, f3{0.1f, 0.25f, -0.15f}),
+                          mat3mul(xC, lightDir, zC, f3{0.2f, 0.5f, 0.2f}),
+                          mat3mul(xC, lightDir, zC, f3{-0.2f, 0.1f, -0.1f}),
+                          mat3mul(xC, lightDir, zC, f3{-0.05f, 0.75f, 0.05f}),
+                          mat3mul(xC, lightDir, zC, f3{-0.1f, 1.0f, 0.0f}),
+                          mat3mul(xC, lightDir, zC, f3{0.0f, 3.0f, 0.0f})};
+    // the step-independent part of the light sample position
+    // pos + ((stepSize * kernel[i]) * i) (cloudRayMarch.comp:656)
+    for (int i = 0; i < 6; ++i) rc.koff[i] = (stepSize * kernel[i]) * (float)i;
+    rc.wind_t = (ld3(p.wind_dir) * p.wind_speed) * tm.time[1];
+    rc.lenInner = length3(startPos - ray.origin);
     rc.skew = ld3(p.skew_dir);
-    rc.total_time = tm.time[1];
 }
 
 struct StepOut {
@@ -145,18 +149,15 @@ template <int S>
 MT_HD StepOut eval_step(const mt_params& p, const Frame& F, const Tex<S>& tx, const mt_time_ubo& tm,
                         const RayConsts& rc, float t) {
     StepOut o{0, 0.0f, 0.0f};
-    int _index = f2i(gmod((float)(rc.pixelID + f2i(t)), 16.0f));
-    float jx, jy;
-    jitter_offset(tm, _index, 1.0f, 1.0f, false, jx, jy);  // halton values; / 75 below
-    jx = rdiv(jx, MT_RCP(0.0f, 75.0f));
-    jy = rdiv(jy, MT_RCP(0.0f, 75.0f));
-    f3 jd = rc.ray.direction + f3{jx, (jx + jy) * 1.180f, jy};
+    const int _index = f2i(gmod((float)(rc.pixelID + f2i(t)), 16.0f));
+    const float* j = rc.jitter[_index & 15];  // _index is in 0..15 for every finite t
+    f3 jd = rc.ray.direction + f3{j[0], j[1], j[2]};
     f3 pos = rc.ray.origin + t * jd;
     f3 sp = relative_position(F, pos, rc.ec);
     sp = f3{rdiv(sp.x, F.r_period), rdiv(sp.y, F.r_period), rdiv(sp.z, F.r_period)};
-    float relH = relative_height(F, pos, rc.ec, rc.startPos, rc.ray.direction, rc.ray.origin);
+    float relH = relative_height(F, pos, rc.ec, rc.lenInner, rc.ray.direction, rc.ray.origin);
     sp = sp + ((relH * rc.skew) * p.cloud_top_offset) * 0.009f;
-    sp = sp + rc.wind * rc.total_time;
+    sp = sp + rc.wind_t;
     Weather wt = weather_at<S>(p, F, tx, pos, rc.ec);
     if (p.height_gradient) wt.hgrad = height_gradient(relH, wt.type);
     // A zero height gradient or zero coverage makes the density 0 (or NaN
@@ -173,7 +174,7 @@ MT_HD StepOut eval_step(const mt_params& p, const Frame& F, const Tex<S>& tx, co
         // instruction cache (the dominant stall when unrolled).
 #pragma unroll 1
         for (int i = 0; i < 6; ++i) {
-            f3 lightPos = pos + ((rc.stepSize * rc.kernel[i]) * (float)i);
+            f3 lightPos = pos + rc.koff[i];
             f3 slp = relative_position(F, lightPos, rc.ec);
             float cbl = sample_low_frequency<S>(p, tx, slp, relH, wt);
             if (cbl > 0.0f) dl = dl + erode(1.5f * cbl, ero);
@@ -191,9 +192,9 @@ MT_HD StepOut eval_step(const mt_params& p, const Frame& F, const Tex<S>& tx, co
 // steps past the exit are discarded.  Result, counters and control flow equal
 // the sequential loop's.
 template <int G, int S>
-MT_HD f3 ray_march_group(const mt_params& p, const Frame& F, const Tex<S>& tx, const mt_time_ubo& tm, const Ray& ray,
-                         f3 ec, f3 startPos, float start_t, float end_t, int pixelID, float& accum, Counts& cnt,
-                         unsigned gmask, int lane) {
+MT_HD f3 ray_march_group(const mt_params& p, const Frame& F, const Tex<S>& tx, const mt_time_ubo& tm,
+                         const float (*jitter)[3], const Ray& ray, f3 ec, f3 startPos, float start_t, float end_t,
+                         int pixelID, float& accum, Counts& cnt, unsigned gmask, int lane) {
     float _dot = dot3(ray.direction, f3{0.0f, 1.0f, 0.0f});
     float maxSteps;
     if (p.steps_min == p.steps_max)
@@ -204,6 +205,7 @@ MT_HD f3 ray_march_group(const mt_params& p, const Frame& F, const Tex<S>& tx, c
     const float stepSize = thick / maxSteps;
     RayConsts rc;
     ray_consts(p, tm, ray, ec, startPos, stepSize, pixelID, rc);
+    rc.jitter = jitter;
     float transmittance = 1.0f;
     f3 color{0.0f, 0.0f, 0.0f};
     // Iteration guard (not in the reference): a step below the ulp of t would
@@ -297,7 +299,8 @@ MT_HD void march_pixel(const MarchArgs& a, const Frame& F, const Tex<S>& tx, int
         out = ray_sphere(ray.origin, ray.direction, ec, F.Rout);
     }
     float accum = 0.0f;
-    f3 res = ray_march_group<G, S>(p, F, tx, a.time, ray, ec, in.point, in.t, out.t, pixelID, accum, cnt, gmask, lane);
+    f3 res = ray_march_group<G, S>(p, F, tx, a.time, a.jitter, ray, ec, in.point, in.t, out.t, pixelID, accum, cnt,
+                                   gmask, lane);
     if (lane != 0) return;
     float godAccum = accum;
     accum = accum * gsmoothstep(0.0f, 1.0f, gmin(1.0f, remap(ray.direction.y, fade, 0.2f, 0.0f, 1.0f)));

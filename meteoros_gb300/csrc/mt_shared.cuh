@@ -160,9 +160,10 @@ MT_HD float remap_clamped_ba(float v, float omin, float omax, float nmin, float 
 }
 
 // cloudRayMarch.comp:171-186
-MT_HD float relative_height(const Frame& F, f3 point, f3 ec, f3 startPos, f3 rayDir, f3 eye) {
+// lenInner = length(startPos - eye) is the same for every step of a ray; the
+// raymarch passes it in precomputed.
+MT_HD float relative_height(const Frame& F, f3 point, f3 ec, float lenInner, f3 rayDir, f3 eye) {
     float lenCam = length3(point - eye);
-    float lenInner = length3(startPos - eye);
     f3 p2e = normalize3_r(point - ec);
     float cosTheta = dot3(rayDir, p2e);
     float num = fabsf(cosTheta * (lenCam - lenInner));
