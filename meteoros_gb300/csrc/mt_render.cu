@@ -101,13 +101,10 @@ MT_HD void txaa_centre(const ViewConsts& v, int x, int y, int W, int H, float& i
 // postProcess_TXAA.frag:223-269 for fragment (x, y); `load(i, j)` reads the
 // current frame (0 outside the image, as imageLoad does).
 template <class Load>
-MT_HD f4v txaa_pixel(const mt_params& p, const ViewConsts& v, const float4* __restrict__ history, int x, int y, int W,
-                     int H, Load load) {
+MT_HD f4v txaa_resolve(const mt_params& p, const ViewConsts& v, f4v prev, int x, int y, int W, int H, Load load) {
     float iux, iuy;
     int ppx, ppy;
     txaa_centre(v, x, y, W, H, iux, iuy, ppx, ppy);
-    float old_u, old_v;
-    old_uv(v, iux, iuy, old_u, old_v);
     f4v ctl = load(ppx - 1, ppy - 1), ctc = load(ppx, ppy - 1), ctr = load(ppx + 1, ppy - 1);
     f4v cml = load(ppx - 1, ppy), cmc = load(ppx, ppy), cmr = load(ppx + 1, ppy);
     f4v cbl = load(ppx - 1, ppy + 1), cbc = load(ppx, ppy + 1), cbr = load(ppx + 1, ppy + 1);
@@ -124,7 +121,6 @@ MT_HD f4v txaa_pixel(const mt_params& p, const ViewConsts& v, const float4* __re
     cmax = f4v{0.5f * (cmax.x + cmax5.x), 0.5f * (cmax.y + cmax5.y), 0.5f * (cmax.z + cmax5.z), 0.5f * (cmax.w + cmax5.w)};
     cavg = f4v{0.5f * (cavg.x + cavg5.x), 0.5f * (cavg.y + cavg5.y), 0.5f * (cavg.z + cavg5.z), 0.5f * (cavg.w + cavg5.w)};
     f4v curr = cmc;
-    f4v prev = tex2_border(history, W, H, old_u, old_v);
     // clip_aabb (:171-191)
     f4v pc = min4(max4(cavg, cmin), cmax);
     f3 p_clip{0.5f * (cmax.x + cmin.x), 0.5f * (cmax.y + cmin.y), 0.5f * (cmax.z + cmin.z)};
@@ -145,6 +141,24 @@ MT_HD f4v txaa_pixel(const mt_params& p, const ViewConsts& v, const float4* __re
     float uw = 1.0f - ud;
     float k = gmix(p.feedback_min, p.feedback_max, uw * uw);
     return mix4(prev, curr, k);
+}
+
+// The history tap of fragment (x, y): the previous resolved frame sampled at
+// the previous camera's uv (postProcess_TXAA.frag:230-249).  It depends on the
+// uniforms and the history only, not on the current frame.
+MT_HD f4v txaa_history(const ViewConsts& v, const float4* __restrict__ history, int x, int y, int W, int H) {
+    float iux, iuy;
+    int ppx, ppy;
+    txaa_centre(v, x, y, W, H, iux, iuy, ppx, ppy);
+    float old_u, old_v;
+    old_uv(v, iux, iuy, old_u, old_v);
+    return tex2_border(history, W, H, old_u, old_v);
+}
+
+template <class Load>
+MT_HD f4v txaa_pixel(const mt_params& p, const ViewConsts& v, const float4* __restrict__ history, int x, int y, int W,
+                     int H, Load load) {
+    return txaa_resolve(p, v, txaa_history(v, history, x, y, W, H), x, y, W, H, load);
 }
 
 // reprojection.comp:193-244 for every pixel the march does not write.
@@ -169,6 +183,19 @@ __global__ void __launch_bounds__(256) reproject_kernel(const __grid_constant__ 
 // one column/row before, two after) in shared memory, zero outside the image
 // as imageLoad returns; the nine taps per pixel then read shared memory.
 constexpr int kTxaaTW = 32, kTxaaTH = 8;
+
+// The history taps of a frame, into `out` (which the resolve then reads back
+// and overwrites, pixel by pixel): run beside the raymarch, since they do not
+// depend on the frame being rendered.
+__global__ void __launch_bounds__(kTxaaTW * kTxaaTH) txaa_history_kernel(const __grid_constant__ TxaaArgs a) {
+    const int x = blockIdx.x * kTxaaTW + threadIdx.x, y = blockIdx.y * kTxaaTH + threadIdx.y;
+    if (x >= a.width || y >= a.height) return;
+    const f4v h = txaa_history(a.vc, a.history, x, y, a.width, a.height);
+    a.out[(size_t)y * (size_t)a.width + (size_t)x] = make_float4(h.x, h.y, h.z, h.w);
+}
+
+// HISTORY_IN_OUT: the history taps were stored in `out` by txaa_history_kernel.
+template <bool HISTORY_IN_OUT>
 __global__ void __launch_bounds__(kTxaaTW * kTxaaTH) txaa_kernel(const __grid_constant__ TxaaArgs a) {
     constexpr int SW = kTxaaTW + 3, SH = kTxaaTH + 3;
     __shared__ float4 tile[SH][SW];
@@ -188,8 +215,16 @@ __global__ void __launch_bounds__(kTxaaTW * kTxaaTH) txaa_kernel(const __grid_co
         const float4 s = tile[j - y0][i - x0];
         return f4v{s.x, s.y, s.z, s.w};
     };
-    const f4v r = txaa_pixel(a.params, a.vc, a.history, x, y, W, H, load);
-    a.out[(size_t)y * (size_t)W + (size_t)x] = make_float4(r.x, r.y, r.z, r.w);
+    const size_t o = (size_t)y * (size_t)W + (size_t)x;
+    f4v prev;
+    if (HISTORY_IN_OUT) {
+        const float4 h = a.out[o];
+        prev = f4v{h.x, h.y, h.z, h.w};
+    } else {
+        prev = txaa_history(a.vc, a.history, x, y, W, H);
+    }
+    const f4v r = txaa_resolve(a.params, a.vc, prev, x, y, W, H, load);
+    a.out[o] = make_float4(r.x, r.y, r.z, r.w);
 }
 
 // Reprojection fused with the TXAA resolve, after the raymarch of the frame.
@@ -317,9 +352,6 @@ constexpr int kResolveTW = 32, kResolveTH = 8;
 cudaError_t launch_frame(const MarchArgs& a, cudaStream_t s, const LaunchEvents* ev, const ForkJoin* fj) {
     const bool timed = ev && ev->on;
     if (!a.fused_resolve) {
-        // reprojection (beside the raymarch when fj is given), raymarch, TXAA
-        cudaError_t e = launch_render(a, s, ev, fj);
-        if (e != cudaSuccess) return e;
         TxaaArgs t;
         t.camera = a.camera;
         t.camera_old = a.camera_old;
@@ -331,7 +363,34 @@ cudaError_t launch_frame(const MarchArgs& a, cudaStream_t s, const LaunchEvents*
         t.width = a.width;
         t.height = a.height;
         t.vc = a.vc_txaa;
-        return launch_txaa(t, s, timed ? ev->resolve : nullptr);
+        if (!fj || (a.flags & MT_RENDER_FULL)) {
+            // reprojection, raymarch, TXAA on one stream
+            cudaError_t e = launch_render(a, s, ev, fj);
+            if (e != cudaSuccess) return e;
+            return launch_txaa(t, s, timed ? ev->resolve : nullptr);
+        }
+        // raymarch on s; beside it on aux the reprojection and the TXAA history
+        // taps; then the TXAA resolve on s
+        const dim3 block(kTxaaTW, kTxaaTH),
+            grid((unsigned)((a.width + kTxaaTW - 1) / kTxaaTW), (unsigned)((a.height + kTxaaTH - 1) / kTxaaTH));
+        cudaError_t e = cudaEventRecord(fj->fork, s);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(fj->aux, fj->fork, 0);
+        if (e == cudaSuccess) e = launch_march(a, s, ev);
+        if (e != cudaSuccess) return e;
+        if (timed) cudaEventRecord(ev->reproject[0], fj->aux);
+        e = launch_reproject(a, fj->aux);
+        if (e == cudaSuccess) {
+            txaa_history_kernel<<<grid, block, 0, fj->aux>>>(t);
+            e = cudaGetLastError();
+        }
+        if (timed) cudaEventRecord(ev->reproject[1], fj->aux);
+        if (e == cudaSuccess) e = cudaEventRecord(fj->join, fj->aux);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s, fj->join, 0);
+        if (e != cudaSuccess) return e;
+        if (timed) cudaEventRecord(ev->resolve[0], s);
+        txaa_kernel<true><<<grid, block, 0, s>>>(t);
+        if (timed) cudaEventRecord(ev->resolve[1], s);
+        return cudaGetLastError();
     }
     cudaError_t e = launch_march(a, s, ev);
     if (e != cudaSuccess) return e;
@@ -352,7 +411,7 @@ cudaError_t launch_txaa(const TxaaArgs& a, cudaStream_t s, const cudaEvent_t* ev
     if (ev) cudaEventRecord(ev[0], s);
     const dim3 block(kTxaaTW, kTxaaTH),
         grid((unsigned)((a.width + kTxaaTW - 1) / kTxaaTW), (unsigned)((a.height + kTxaaTH - 1) / kTxaaTH));
-    txaa_kernel<<<grid, block, 0, s>>>(a);
+    txaa_kernel<false><<<grid, block, 0, s>>>(a);
     if (ev) cudaEventRecord(ev[1], s);
     return cudaGetLastError();
 }
