@@ -20,6 +20,7 @@ MT_DETAIL_N = 32
 MT_CURL_N = 128
 MT_WEATHER_N = 512
 MT_MAX_WEATHER_SLOTS = 256
+MT_MAX_DIM = 16384
 MT_NOALLOC_MAX_VIEWS = 64
 MT_LDR_RGBA8 = 0
 MT_VOLUME_BASE = 0

@@ -138,8 +138,9 @@ void CUDART_CB on_batch_done(void* data) {
 bool can_form_batch(mt_server* s) {
     if (s->pending.empty() || s->inflight >= s->cfg.streams) return false;
     for (uint64_t id : s->pending) {
-        const Request& r = s->requests[id];
-        auto it = s->sessions.find(r.session);
+        auto rq = s->requests.find(id);
+        if (rq == s->requests.end()) return true;  // dropped by the next pass
+        auto it = s->sessions.find(rq->second.session);
         if (it == s->sessions.end() || !it->second.busy) return true;
     }
     return false;
@@ -157,7 +158,9 @@ void worker_main(mt_server* s) {
         std::deque<uint64_t> keep;
         const int max_batch = s->cfg.per_request ? 1 : std::max(1, s->cfg.max_batch);
         for (uint64_t id : s->pending) {
-            Request& r = s->requests[id];
+            auto rq = s->requests.find(id);
+            if (rq == s->requests.end()) continue;
+            Request& r = rq->second;
             auto it = s->sessions.find(r.session);
             if (it == s->sessions.end()) {  // session closed: fail the request
                 r.status = MT_ERR_INVALID_ARG;

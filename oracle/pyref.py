@@ -124,8 +124,8 @@ def stbi_available() -> bool:
 
 
 def stbi_load_rgba(data: bytes) -> np.ndarray | None:
-    """The reference's stb_image decode of a TGA file to (H, W, 4) RGBA8
-    (None when stb_image rejects it)."""
+    """The reference's stb_image decode of a TGA or PNG file to (H, W, 4)
+    RGBA8 (None when stb_image rejects it)."""
     global _stbi
     if _stbi is None:
         path = ref_build.build_stbi()
@@ -138,7 +138,10 @@ def stbi_load_rgba(data: bytes) -> np.ndarray | None:
         _stbi = L
     buf = np.frombuffer(data, np.uint8)
     w, h = C.c_int(), C.c_int()
-    cap = 4 * (data[12] | data[13] << 8) * (data[14] | data[15] << 8) if len(data) >= 18 else 0
+    if data[:8] == b"\x89PNG\r\n\x1a\n" and len(data) >= 24:  # IHDR width, height (big-endian)
+        cap = 4 * int.from_bytes(data[16:20], "big") * int.from_bytes(data[20:24], "big")
+    else:  # TGA header width, height (little-endian)
+        cap = 4 * (data[12] | data[13] << 8) * (data[14] | data[15] << 8) if len(data) >= 18 else 0
     cap = max(cap, 4)
     out = np.zeros(cap, np.uint8)
     rc = _stbi.ref_stbi_load_rgba(_p(buf), len(data), C.byref(w), C.byref(h), _p(out), cap)

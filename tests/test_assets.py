@@ -81,3 +81,32 @@ def test_shipped_volumes_match_golden_hashes(oracle, stbi, golden):
     for kind, n, key in (("LowFrequency", 128, "tga_sha256_base"), ("HighFrequency", 32, "tga_sha256_detail")):
         vol = shipped_volume(oracle.decode_tga, kind, n)
         assert hashlib.sha256(vol.tobytes()).digest() == golden[key].tobytes(), kind
+
+
+def test_ref_frame_with_shipped_assets_matches_reference_source(oracle, stbi):
+    """The REF preset on the reference's own noise assets (TGA slices decoded
+    by the restatement, curl and weather maps by the reference's stb_image):
+    the restatement's frame equals the reference shader source's, bit for bit."""
+    from meteoros_gb300 import abi
+    from oracle import pyref
+
+    base = shipped_volume(oracle.decode_tga, "LowFrequency", 128)
+    detail = shipped_volume(oracle.decode_tga, "HighFrequency", 32)
+    curl = stbi.stbi_load_rgba((REF_TEXTURES / "curlNoise.png").read_bytes())
+    weather = stbi.stbi_load_rgba((REF_TEXTURES / "weatherMap.png").read_bytes())
+    assert base.shape == (128, 128, 128, 4) and detail.shape == (32, 32, 32, 4)
+    assert curl.shape == (128, 128, 4) and weather.shape == (512, 512, 4)
+    vol = oracle.Volumes(base, detail, curl, weather)
+    w, h = 72, 40
+    prev = np.random.default_rng(9).random((h, w, 4), dtype=np.float32)
+    for pitch, slot in ((5.0, 3), (25.0, 12)):
+        cam = __import__("meteoros_gb300.scenes", fromlist=["look"]).look((0.0, 0.0, 2.0), 10.0, pitch, 45.0, w, h)
+        tm = abi.time_init()
+        tm.frame_count_mod16 = slot
+        tm.time[1] = 3.5
+        a, am, _ = oracle.render(vol, cam, cam, tm, abi.params_reference(), prev, w, h, 0)
+        b, bm = pyref.frame(vol, cam, cam, tm, prev, w, h)
+        for x, y, what in ((a, b, "rgba"), (am, bm, "mask")):
+            na, nb = np.isnan(x), np.isnan(y)
+            assert np.array_equal(na, nb), what
+            assert np.array_equal(np.where(na, 0, x).view(np.uint32), np.where(nb, 0, y).view(np.uint32)), what

@@ -179,6 +179,24 @@ def test_edge_sizes(ctx, oracle, volumes_seed7, size):
     check_frame(oracle, vol, ctx, cam, cam, tm, params, None, w, h, abi.MT_RENDER_FULL, f"{w}x{h} full")
 
 
+@pytest.mark.parametrize("size", [(abi.MT_MAX_DIM, 8), (8, abi.MT_MAX_DIM)])
+def test_maximum_dimensions(ctx, oracle, volumes_seed7, size):
+    """The largest width and height the ABI accepts (index arithmetic at the
+    limit); one above is rejected."""
+    vol = oracle.Volumes(volumes_seed7["base"], volumes_seed7["detail"], volumes_seed7["curl"],
+                         volumes_seed7["weather"])
+    w, h = size
+    cam, tm, params, _ = scenes.config_view(9, w, h)
+    prev = np.random.default_rng(5).random((h, w, 4), dtype=np.float32)
+    tm.frame_count_mod16 = 6
+    check_frame(oracle, vol, ctx, cam, cam, tm, params, prev, w, h, 0, f"{w}x{h} checkerboard")
+    check_frame(oracle, vol, ctx, cam, cam, tm, params, None, w, h, abi.MT_RENDER_FULL, f"{w}x{h} full")
+    big = torch.zeros((h, w + 1, 4) if w > h else (h + 1, w, 4), dtype=torch.float32, device="cuda")
+    with pytest.raises(abi.MeteorosError) as e:
+        ctx.render(cam, cam, tm, params, None, big, None, abi.MT_RENDER_FULL)
+    assert e.value.status == abi.MT_ERR_INVALID_ARG
+
+
 def test_deterministic(ctx):
     w, h = 256, 144
     cam, tm, params, _ = scenes.config_view(4, w, h)
