@@ -386,7 +386,8 @@ MT_API mt_status mt_get_kernel_times(mt_ctx* ctx, mt_kernel_times* out);
  * by anything else while the server exists.  A session keeps its two raw
  * frames (the reprojection ping-pong, Renderer.cpp:131-136), its god-ray
  * mask and its previous camera resident in HBM; sessions are admitted while
- * width * height * 36 bytes each fit hbm_budget_bytes (else MT_ERR_BUDGET).
+ * width * height * 36 bytes each fit hbm_budget_bytes (after waiting up to
+ * admission_wait_ms for sessions to close; else MT_ERR_BUDGET).
  * Each request is one frame of one session: the first marches every pixel,
  * later ones march one pixel per 4x4 block and reproject the previous frame.
  * A batch takes every queued request whose session has no frame in flight
@@ -404,7 +405,8 @@ typedef struct mt_server_config {
                                    per-request launch the batched loop is compared with) */
     int32_t use_graph;          /* 1 = each batch as a CUDA graph; 0 = direct launches (lower
                                    host cost per batch) */
-    int32_t _reserved[1];
+    int32_t admission_wait_ms;  /* mt_server_open_session waits up to this long for closing
+                                   sessions to free budget before MT_ERR_BUDGET (0 = no wait) */
 } mt_server_config;
 
 typedef struct mt_request_info {

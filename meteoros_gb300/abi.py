@@ -143,7 +143,7 @@ class View(C.Structure):
 class ServerConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_batch", C.c_int32), ("streams", C.c_int32),
                 ("batch_lanes", C.c_int32), ("per_request", C.c_int32), ("use_graph", C.c_int32),
-                ("_reserved", C.c_int32 * 1)]
+                ("admission_wait_ms", C.c_int32)]
 
 
 class RequestInfo(C.Structure):

@@ -307,8 +307,13 @@ MT_API mt_status mt_server_open_session(mt_server* s, int width, int height, con
         // reserve the budget; allocation happens outside the lock (a CUDA
         // call that waits for the device must not hold the lock the
         // completion callbacks take)
-        std::lock_guard<std::mutex> lk(s->mu);
-        if (s->used_bytes + bytes > s->cfg.hbm_budget_bytes)
+        std::unique_lock<std::mutex> lk(s->mu);
+        if (bytes > s->cfg.hbm_budget_bytes)
+            return sfail(s, MT_ERR_BUDGET, "session is larger than the HBM budget");
+        // admitted when closing sessions free enough of the budget, within the wait
+        const auto fits = [&] { return s->used_bytes + bytes <= s->cfg.hbm_budget_bytes; };
+        if (!fits() && !(s->cfg.admission_wait_ms > 0 &&
+                         s->cv_done.wait_for(lk, std::chrono::milliseconds(s->cfg.admission_wait_ms), fits)))
             return sfail(s, MT_ERR_BUDGET, "session does not fit the HBM budget");
         s->used_bytes += bytes;
     }
@@ -353,8 +358,11 @@ MT_API mt_status mt_server_close_session(mt_server* s, int64_t session) {
     cudaFree(se.raw[0]);
     cudaFree(se.raw[1]);
     cudaFree(se.mask);
-    std::lock_guard<std::mutex> lk(s->mu);
-    s->used_bytes -= se.bytes;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->used_bytes -= se.bytes;
+    }
+    s->cv_done.notify_all();  // budget freed: a waiting admission may proceed
     return MT_OK;
 }
 

@@ -33,7 +33,8 @@ class RequestInfo:
 
 class Server:
     def __init__(self, ctx, max_batch: int = 64, streams: int = 2, hbm_budget_bytes: int = 40 << 30,
-                 batch_lanes: int = 0, per_request: bool = False, use_graph: bool = False):
+                 batch_lanes: int = 0, per_request: bool = False, use_graph: bool = False,
+                 admission_wait_ms: int = 0):
         self.ctx = ctx
         self.lib = ctx.lib
         cfg = abi.ServerConfig()
@@ -43,6 +44,7 @@ class Server:
         cfg.batch_lanes = int(batch_lanes)
         cfg.per_request = 1 if per_request else 0
         cfg.use_graph = 1 if use_graph else 0
+        cfg.admission_wait_ms = int(admission_wait_ms)
         h = C.c_void_p()
         st = self.lib.mt_server_create(ctx.handle, C.byref(cfg), C.byref(h))
         if st != abi.MT_OK:

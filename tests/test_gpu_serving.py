@@ -153,3 +153,30 @@ def test_continuous_batching_overlaps_batches(ctx):
         assert len(batches) >= n // 8
         overlapped = any(b[0] < a[1] for a, b in zip(batches, batches[1:]))
         assert overlapped, "no batch started while the previous one ran"
+
+
+def test_admission_waits_for_budget_to_free(ctx):
+    """With admission_wait_ms, a session that does not fit is admitted once a
+    closing session frees the budget; without a close it fails after the wait."""
+    import threading
+    import time
+
+    from meteoros_gb300.server import Server
+
+    _, _, params, _ = scenes.config_view(2, 320, 180)
+    per_session = 320 * 180 * (2 * 16 + 4)
+    with Server(ctx, hbm_budget_bytes=2 * per_session, admission_wait_ms=3000) as srv:
+        a = srv.open_session(320, 180, params)
+        srv.open_session(320, 180, params)
+        closer = threading.Timer(0.2, lambda: srv.close_session(a))
+        t0 = time.perf_counter()
+        closer.start()
+        srv.open_session(320, 180, params)  # waits for the close
+        waited = time.perf_counter() - t0
+        closer.join()
+        assert 0.1 < waited < 3.0
+    with Server(ctx, hbm_budget_bytes=per_session, admission_wait_ms=100) as srv:
+        srv.open_session(320, 180, params)
+        with pytest.raises(abi.MeteorosError) as e:
+            srv.open_session(320, 180, params)
+        assert e.value.status == abi.MT_ERR_BUDGET
