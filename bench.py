@@ -545,7 +545,8 @@ def run_gb300(args) -> int:
         "clocks": clk,
         "e2e": {"value": round(e2e_ms, 4), "unit": UNIT, "h2d_bytes_per_step": ubo_bytes,
                 "d2h_bytes_per_step": d2h},
-        "gpu_launches": 3 * args.steps,
+        # per frame: raymarch, reprojection, TXAA history taps, TXAA resolve
+        "gpu_launches": 4 * args.steps,
         "wall_s_timed": round(wall, 3),
         "cpu_baseline": cpu,
         "forms": forms,
