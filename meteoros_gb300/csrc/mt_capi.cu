@@ -39,6 +39,7 @@ struct mt_ctx {
     bool ran[4] = {false, false, false, false};
     int march_lanes = 0;                      // step-parallel lanes per ray (mt_set_tuning); 0 = auto
     int march_block = 128;                    // march_kernel CTA size (mt_set_tuning)
+    int march_order = 0;                      // 0: horizon rows first; 1: top to bottom
     int fused_resolve = 0;                    // mt_render_frame: reprojection fused with TXAA
     // mt_render_batch
     int batch_tile_w = 16, batch_tile_h = 8, batch_lanes = 1;
@@ -210,6 +211,7 @@ mt_status build_march_args(mt_ctx* ctx, const mt_camera_ubo* cam, const mt_camer
     mt::make_view_consts(&a->vc_repro, *p, *cam, *cam_old, *tm, w, h, true);
     mt::make_view_consts(&a->vc_txaa, *p, *cam, *cam_old, *tm, w, h, false);
     mt::make_march_jitter(a->jitter, *tm);
+    a->row_pivot = ctx->march_order == 0 ? mt::march_row_pivot(*p, *cam, w, h, full) : -1;
     a->lanes = ctx->march_lanes;
     if (a->lanes == 0) {
         // Auto: enough rays fill the GPU one lane per ray; fewer rays (a
@@ -697,8 +699,13 @@ MT_API mt_status mt_render_batch(mt_ctx* ctx, const mt_view* views, int n_views,
     for (int i : order) {
         int nx, ny;
         ray_grid(args[(size_t)i], &nx, &ny);
-        for (int y = 0; y < ny; y += th)
+        // tile rows from the view's horizon up, then the rows below it (march_row)
+        const int nty = (ny + th - 1) / th;
+        const int pt = args[(size_t)i].row_pivot >= 0 ? std::min(args[(size_t)i].row_pivot / th, nty - 1) : -1;
+        for (int k = 0; k < nty; ++k) {
+            const int y = mt::march_row(k, pt) * th;
             for (int x = 0; x < nx; x += tw) tiles.push_back(mt::BatchTile{i, x, y, nx, ny});
+        }
     }
     if ((st = ensure_batch_buffers(ctx, (size_t)n_views, tiles.size())) != MT_OK) return st;
     // Slot: the batch that used it last (two calls ago) must have finished
@@ -871,6 +878,7 @@ MT_API mt_status mt_set_tuning(mt_ctx* ctx, const mt_tuning* t) {
         return fail(ctx, MT_ERR_INVALID_ARG, "reproject_serial must be 0 or 1");
     if (t->march_block != 0 && t->march_block != 32 && t->march_block != 128)
         return fail(ctx, MT_ERR_INVALID_ARG, "march_block must be 0 (default 128), 32 or 128");
+    if (t->march_order != 0 && t->march_order != 1) return fail(ctx, MT_ERR_INVALID_ARG, "march_order must be 0 or 1");
     ctx->march_lanes = t->march_lanes;
     ctx->fused_resolve = t->fused_resolve;
     ctx->batch_tile_w = t->batch_tile_w;
@@ -879,6 +887,7 @@ MT_API mt_status mt_set_tuning(mt_ctx* ctx, const mt_tuning* t) {
     ctx->batch_direct = t->batch_direct;
     ctx->overlap = t->reproject_serial ? 0 : 1;
     ctx->march_block = t->march_block == 0 ? 128 : t->march_block;
+    ctx->march_order = t->march_order;
     return MT_OK;
 }
 
@@ -894,6 +903,7 @@ MT_API mt_status mt_get_tuning(mt_ctx* ctx, mt_tuning* t) {
     t->batch_direct = ctx->batch_direct;
     t->reproject_serial = ctx->overlap ? 0 : 1;
     t->march_block = ctx->march_block;
+    t->march_order = ctx->march_order;
     return MT_OK;
 }
 
@@ -1041,8 +1051,12 @@ MT_API mt_status mt_render_batch_noalloc(mt_ctx* ctx, const mt_view* views, int 
         const int i = order[o];
         int nx, ny;
         ray_grid(args[i], &nx, &ny);
-        for (int y = 0; y < ny; y += th)
+        const int nty = (ny + th - 1) / th;
+        const int pt = args[i].row_pivot >= 0 ? std::min(args[i].row_pivot / th, nty - 1) : -1;
+        for (int k = 0; k < nty; ++k) {
+            const int y = mt::march_row(k, pt) * th;
             for (int x = 0; x < nx; x += tw) tiles[t++] = mt::BatchTile{i, x, y, nx, ny};
+        }
     }
     // The work counter must start at zero: it is part of the first copy.
     std::memset(g_noalloc_host, 0, kNoallocViewsOff);

@@ -154,7 +154,7 @@ class Context:
     def set_tuning(self, march_lanes: int | None = None, fused_resolve: bool | None = None,
                    batch_tile: tuple[int, int] | None = None, batch_lanes: int | None = None,
                    batch_direct: bool | None = None, reproject_serial: bool | None = None,
-                   march_block: int | None = None) -> abi.Tuning:
+                   march_block: int | None = None, march_order: int | None = None) -> abi.Tuning:
         t = abi.Tuning()
         self._check(self.lib.mt_get_tuning(self.handle, C.byref(t)))
         if march_lanes is not None:
@@ -171,6 +171,8 @@ class Context:
             t.reproject_serial = 1 if reproject_serial else 0
         if march_block is not None:
             t.march_block = march_block
+        if march_order is not None:
+            t.march_order = march_order
         self._check(self.lib.mt_set_tuning(self.handle, C.byref(t)))
         return t
 

@@ -271,6 +271,31 @@ def test_march_lane_counts_give_identical_frames(ctx, lanes):
         assert a[2] == b[2]
 
 
+@pytest.mark.parametrize("pitch", [-20.0, 0.0, 12.0, 45.0, 80.0])
+def test_row_dispatch_order_gives_identical_frames(ctx, pitch):
+    """Horizon-first ray-row order and top-to-bottom order give the same bits
+    and counters, whatever the horizon's place in the image (or its absence)."""
+    w, h = 256, 200
+    cam = scenes.look((0.0, 100.0, 0.0), 30.0, pitch, 60.0, w, h)
+    _, tm, params, _ = scenes.config_view(22, w, h)
+    prev = to_dev(np.random.default_rng(2).random((h, w, 4), dtype=np.float32), torch)
+    outs = []
+    for order in (1, 0):
+        ctx.set_tuning(march_order=order)
+        for flags in (abi.MT_RENDER_FULL, abi.MT_RENDER_CHECKERBOARD):
+            cur = torch.zeros((h, w, 4), dtype=torch.float32, device="cuda")
+            mask = torch.full((h, w), float("nan"), dtype=torch.float32, device="cuda")
+            ctx.render(cam, cam, tm, params, prev, cur, mask, flags | abi.MT_RENDER_COUNT)
+            st = ctx.stats(reset=True)
+            outs.append((cur.cpu().numpy(), mask.cpu().numpy(),
+                         (st.primary_samples, st.light_samples, st.marched_rays, st.pixels)))
+    ctx.set_tuning(march_order=0)
+    for a, b in zip(outs[:2], outs[2:]):
+        assert_bits_equal(a[0], b[0], f"pitch {pitch} rgba")
+        assert_bits_equal(a[1], b[1], f"pitch {pitch} mask")
+        assert a[2] == b[2]
+
+
 def test_reciprocal_division_is_ieee_exact(ctx):
     """The kernels divide by reused denominators through a correctly rounded
     reciprocal plus one correction step; it must equal IEEE division bit for bit."""
