@@ -39,7 +39,7 @@ struct mt_ctx {
     bool ran[4] = {false, false, false, false};
     int march_lanes = 0;                      // step-parallel lanes per ray (mt_set_tuning); 0 = auto
     int march_block = 128;                    // march_kernel CTA size (mt_set_tuning)
-    int march_order = 0;                      // 0: horizon rows first; 1: top to bottom
+    int march_order = 0;                      // ray rows: 0 bottom to top, 1 top to bottom
     int fused_resolve = 0;                    // mt_render_frame: reprojection fused with TXAA
     // mt_render_batch
     int batch_tile_w = 16, batch_tile_h = 8, batch_lanes = 1;
@@ -211,7 +211,7 @@ mt_status build_march_args(mt_ctx* ctx, const mt_camera_ubo* cam, const mt_camer
     mt::make_view_consts(&a->vc_repro, *p, *cam, *cam_old, *tm, w, h, true);
     mt::make_view_consts(&a->vc_txaa, *p, *cam, *cam_old, *tm, w, h, false);
     mt::make_march_jitter(a->jitter, *tm);
-    a->row_pivot = ctx->march_order == 0 ? mt::march_row_pivot(*p, *cam, w, h, full) : -1;
+    a->bottom_up = ctx->march_order == 0 ? 1 : 0;
     a->lanes = ctx->march_lanes;
     if (a->lanes == 0) {
         // Auto: enough rays fill the GPU one lane per ray; fewer rays (a
@@ -699,11 +699,10 @@ MT_API mt_status mt_render_batch(mt_ctx* ctx, const mt_view* views, int n_views,
     for (int i : order) {
         int nx, ny;
         ray_grid(args[(size_t)i], &nx, &ny);
-        // tile rows from the view's horizon up, then the rows below it (march_row)
+        // tile rows in the view's ray-row order (march_row)
         const int nty = (ny + th - 1) / th;
-        const int pt = args[(size_t)i].row_pivot >= 0 ? std::min(args[(size_t)i].row_pivot / th, nty - 1) : -1;
         for (int k = 0; k < nty; ++k) {
-            const int y = mt::march_row(k, pt) * th;
+            const int y = mt::march_row(k, nty, args[(size_t)i].bottom_up != 0) * th;
             for (int x = 0; x < nx; x += tw) tiles.push_back(mt::BatchTile{i, x, y, nx, ny});
         }
     }
@@ -1052,9 +1051,8 @@ MT_API mt_status mt_render_batch_noalloc(mt_ctx* ctx, const mt_view* views, int 
         int nx, ny;
         ray_grid(args[i], &nx, &ny);
         const int nty = (ny + th - 1) / th;
-        const int pt = args[i].row_pivot >= 0 ? std::min(args[i].row_pivot / th, nty - 1) : -1;
         for (int k = 0; k < nty; ++k) {
-            const int y = mt::march_row(k, pt) * th;
+            const int y = mt::march_row(k, nty, args[i].bottom_up != 0) * th;
             for (int x = 0; x < nx; x += tw) tiles[t++] = mt::BatchTile{i, x, y, nx, ny};
         }
     }

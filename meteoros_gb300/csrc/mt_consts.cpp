@@ -83,27 +83,4 @@ void make_march_jitter(float out[16][3], const mt_time_ubo& tm) {
     }
 }
 
-int march_row_pivot(const mt_params& p, const mt_camera_ubo& cam, int W, int H, bool full) {
-    // Centre-column ray of each row, as cast_ray builds it (no jitter; an
-    // estimate for the dispatch order only, in double).
-    (void)p;
-    const float* m = cam.view;
-    const double ll = std::sqrt((double)m[2] * m[2] + (double)m[6] * m[6] + (double)m[10] * m[10]);
-    const double lx = -m[2] / ll, ly = -m[6] / ll, lz = -m[10] / ll;
-    const double ux = m[1], uy = m[5], uz = m[9];
-    const double ul = std::sqrt(ux * ux + uy * uy + uz * uz);
-    const int rows = full ? H : 32 * ((H / 4 + 31) / 32);
-    const double fade = 0.06;  // cloudRayMarch.comp's fade elevation: lower rays do not march
-    int pivot = -1;
-    for (int r = 0; r < rows; ++r) {
-        const double py = full ? r + 0.5 : 4.0 * r + 2.0;
-        const double ny = (1.0 - py / H) * 2.0 - 1.0;
-        const double s = ny * cam.tan_fov_by_2[1] / ul;
-        const double dx = lx + s * ux, dy = ly + s * uy, dz = lz + s * uz;
-        const double dirY = dy / std::sqrt(dx * dx + dy * dy + dz * dz);
-        if (dirY >= fade) pivot = r;  // rows run top to bottom: keep the lowest one above the fade
-    }
-    return pivot;
-}
-
 }  // namespace mt

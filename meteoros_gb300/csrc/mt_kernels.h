@@ -46,11 +46,11 @@ struct MarchArgs {
     int32_t lanes;               // lanes marching one ray together: 1, 4, 8 or 16
     int32_t block;               // march_kernel CTA size: 32 or 128 threads
     // Dispatch order of the ray rows (rows of 4x4 blocks, or of pixels for a
-    // full frame): row_pivot, row_pivot - 1, ..., 0, then row_pivot + 1, ...
-    // (-1: top to bottom).  The host puts the lowest row that still marches
-    // the cloud layer first -- the longest, costliest rays near the horizon --
-    // so that the cheap rows fill the end of the launch.
-    int32_t row_pivot;
+    // full frame): 1 = bottom to top (default), 0 = top to bottom.  Bottom to
+    // top runs the rows that do not march (below the fade elevation, 10-50x
+    // cheaper) first, which lets the work beside the raymarch start early,
+    // then the marching rows from the horizon up.
+    int32_t bottom_up;
     const float4* history;       // mt_render_frame only: previous resolved frame
     float4* out;                 // mt_render_frame only: resolved frame
     int32_t fused_resolve;       // mt_render_frame: 1 = reprojection fused with TXAA
@@ -64,15 +64,8 @@ struct MarchArgs {
 
 void make_march_jitter(float out[16][3], const mt_time_ubo& tm);
 
-// The row_pivot above for a view: the lowest ray row (largest index) whose
-// centre ray looks above the march's fade elevation, or -1 when none does.
-int march_row_pivot(const mt_params& p, const mt_camera_ubo& cam, int W, int H, bool full);
-
-// The k-th ray row in the dispatch order of row_pivot: a permutation of
-// 0..n-1 for any pivot below n.
-__host__ __device__ inline int march_row(int k, int pivot) {
-    return (pivot >= 0 && k <= pivot) ? pivot - k : k;
-}
+// The k-th of n ray rows in dispatch order.
+__host__ __device__ inline int march_row(int k, int n, bool bottom_up) { return bottom_up ? n - 1 - k : k; }
 
 struct TxaaArgs {
     mt_camera_ubo camera;

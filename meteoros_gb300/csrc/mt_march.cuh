@@ -332,14 +332,14 @@ __global__ void __launch_bounds__(BS, 1024 / BS) march_kernel(const __grid_const
         active = (long long)idx < (long long)a.width * a.height;
         if (active) {
             px = (int)(idx % (unsigned)a.width);
-            py = march_row((int)(idx / (unsigned)a.width), a.row_pivot);
+            py = march_row((int)(idx / (unsigned)a.width), a.height, a.bottom_up);
         }
     } else {
         active = (long long)idx < (long long)a.groups_x * a.groups_y;
         if (active) {
             const int id = a.time.frame_count_mod16;
             px = (int)(idx % (unsigned)a.groups_x) * 4 + a.params.slot_x[id];
-            py = march_row((int)(idx / (unsigned)a.groups_x), a.row_pivot) * 4 + a.params.slot_y[id];
+            py = march_row((int)(idx / (unsigned)a.groups_x), a.groups_y, a.bottom_up) * 4 + a.params.slot_y[id];
             active = px < a.width && py < a.height;
         }
     }

@@ -273,7 +273,7 @@ def test_march_lane_counts_give_identical_frames(ctx, lanes):
 
 @pytest.mark.parametrize("pitch", [-20.0, 0.0, 12.0, 45.0, 80.0])
 def test_row_dispatch_order_gives_identical_frames(ctx, pitch):
-    """Horizon-first ray-row order and top-to-bottom order give the same bits
+    """Bottom-to-top ray-row order and top-to-bottom order give the same bits
     and counters, whatever the horizon's place in the image (or its absence)."""
     w, h = 256, 200
     cam = scenes.look((0.0, 100.0, 0.0), 30.0, pitch, 60.0, w, h)
