@@ -66,8 +66,9 @@ MT_HD int f2i(float v) { return __float2int_rz(v); }
 // r = a - q0*b is exact in one FMA and q = RN(q0 + r*y) is the correctly
 // rounded quotient (Markstein, "Computation of elementary functions on the
 // IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1), 1990).  The
-// theorem excludes overflow and underflow, so zero, tiny, huge and non-finite
-// quotients (and the sign of a zero quotient) go through the IEEE division.
+// theorem excludes overflow and underflow, so tiny, huge and non-finite
+// quotients go through the IEEE division; a zero dividend takes q0, which
+// carries the quotient's sign when y is finite.
 // ---------------------------------------------------------------------------
 struct Rcp {
     float b, y;
@@ -76,13 +77,29 @@ struct Rcp {
 // the instruction cache (the march loop is instruction-fetch bound otherwise).
 static __device__ __noinline__ float div_ieee(float a, float b) { return a / b; }
 MT_HD Rcp make_rcp(float b) { return Rcp{b, div_ieee(1.0f, b)}; }
-MT_HD float rdiv(float a, Rcp r) {
+MT_HD float rdiv_core(float a, Rcp r) {
     const float q0 = __fmul_rn(a, r.y);
-    const float e = __fmaf_rn(-q0, r.b, a);
-    const float q = __fmaf_rn(e, r.y, q0);
+    return __fmaf_rn(__fmaf_rn(-q0, r.b, a), r.y, q0);
+}
+MT_HD bool rdiv_in_range(float q) {
     const float aq = fabsf(q);
-    if (aq >= 0x1p-100f && aq <= 0x1p100f) return q;
+    return aq >= 0x1p-100f && aq <= 0x1p100f;
+}
+MT_HD float rdiv(float a, Rcp r) {
+    const float q = rdiv_core(a, r);
+    if (rdiv_in_range(q)) return q;
+    if (a == 0.0f && fabsf(r.y) <= 0x1.fffffep127f) return __fmul_rn(a, r.y);
     return div_ieee(a, r.b);
+}
+// Three quotients by one denominator with one range check; when any falls
+// outside it, all three are redone one by one out of line.
+static __device__ __noinline__ f3 rdiv3_exceptional(float ax, float ay, float az, Rcp r) {
+    return f3{rdiv(ax, r), rdiv(ay, r), rdiv(az, r)};
+}
+MT_HD f3 rdiv3(f3 a, Rcp r) {
+    const f3 q{rdiv_core(a.x, r), rdiv_core(a.y, r), rdiv_core(a.z, r)};
+    if (rdiv_in_range(q.x) & rdiv_in_range(q.y) & rdiv_in_range(q.z)) return q;
+    return rdiv3_exceptional(a.x, a.y, a.z, r);
 }
 static __device__ __noinline__ float pow_nl(float x, float y) { return powf(x, y); }
 
@@ -112,6 +129,36 @@ MT_HD f4v lerp4(f4v p, f4v q, float t) {
     return f4v{lerp1(p.x, q.x, t), lerp1(p.y, q.y, t), lerp1(p.z, q.z, t), lerp1(p.w, q.w, t)};
 }
 
+// ---------------------------------------------------------------------------
+// Packed FP32 pairs: the f32x2 add and multiply-add instructions of sm_100 and
+// later carry two values per instruction, each half rounded exactly like the
+// scalar operation.  The compiler contracts a packed multiply whose only use
+// is a packed add into one fused multiply-add (one rounding instead of two),
+// with contraction disabled and explicit round-to-nearest alike, so products
+// are formed as fma(a, b, z) with z = -0 read from constant memory:
+// fma(a, b, -0) = RN(a * b) for every a and b (signed zeros, infinities and
+// NaN included), and an addend unknown to the compiler leaves nothing to
+// contract.
+// ---------------------------------------------------------------------------
+static __constant__ float kNegZero2[2] = {-0.0f, -0.0f};
+MT_HD float2 splat2(float v) { return make_float2(v, v); }
+MT_HD float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+// a - b as RN(-1 * b + a): the product is exact, so the one rounding is that of a - b.
+MT_HD float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a); }
+MT_HD float2 mul2(float2 a, float2 b) { return __ffma2_rn(a, b, make_float2(kNegZero2[0], kNegZero2[1])); }
+// p + t * (q - p), each operation rounded (lerp1 on both halves)
+MT_HD float2 lerp2(float2 p, float2 q, float2 t) { return add2(p, mul2(t, sub2(q, p))); }
+
+// Four channels as two packed pairs (x, y) and (z, w).
+struct f4p {
+    float2 xy, zw;
+};
+MT_HD f4p lerp4p(f4p p, f4p q, float2 t) { return f4p{lerp2(p.xy, q.xy, t), lerp2(p.zw, q.zw, t)}; }
+MT_HD f4v scale4p(f4p c, float s) {
+    const float2 xy = mul2(c.xy, splat2(s)), zw = mul2(c.zw, splat2(s));
+    return f4v{xy.x, xy.y, zw.x, zw.y};
+}
+
 // A texel byte as a float without a conversion instruction: byte_perm builds
 // the word 0x4B0000bb, which is the float 2^23 + bb exactly (the byte lands in
 // the low mantissa bits).  Interpolation works on these biased values:
@@ -119,24 +166,23 @@ MT_HD f4v lerp4(f4v p, f4v q, float t) {
 // is reproduced bit for bit.
 MT_HD float biased_byte(uint32_t word, unsigned c) { return __int_as_float(__byte_perm(word, 0x4B000000u, 0x7540u | c)); }
 constexpr float kByteBias = 8388608.0f;
+MT_HD float2 biased_pair(uint32_t word, unsigned c) { return make_float2(biased_byte(word, c), biased_byte(word, c + 1u)); }
 
-MT_HD f4v lerp_texels(uint32_t w0, uint32_t w1, float t) {
-    f4v r;
-    float* o = &r.x;
-#pragma unroll
-    for (unsigned c = 0; c < 4; ++c) {
-        const float P = biased_byte(w0, c), Q = biased_byte(w1, c);
-        o[c] = (P - kByteBias) + t * (Q - P);
-    }
-    return r;
+// The x interpolation of two RGBA8 texels, (P - 2^23) + t * (Q - P) per channel.
+MT_HD f4p lerp_texels(uint32_t w0, uint32_t w1, float2 t) {
+    const float2 bias = splat2(kByteBias);
+    const float2 P0 = biased_pair(w0, 0u), Q0 = biased_pair(w1, 0u);
+    const float2 P1 = biased_pair(w0, 2u), Q1 = biased_pair(w1, 2u);
+    return f4p{add2(sub2(P0, bias), mul2(t, sub2(Q0, P0))), add2(sub2(P1, bias), mul2(t, sub2(Q1, P1)))};
 }
 
 // ---------------------------------------------------------------------------
 // Samplers.  Vulkan LINEAR filter with exact FP32 weights: u = s*N - 0.5,
 // i0 = floor(u), alpha = u - i0, REPEAT wraps the integer texel coordinate
 // (N is a power of two).  Raw texel values are interpolated x, then y, then
-// z, and the result is scaled once (1/255 for UNORM8).  The volumes are
-// RGBA8 words, x fastest, then y, then z (ImageLoadingUtility.cpp:75-139).
+// z, and the result is scaled once (1/255 for UNORM8), channels in packed
+// pairs.  The volumes are RGBA8 words, x fastest, then y, then z
+// (ImageLoadingUtility.cpp:75-139).
 // ---------------------------------------------------------------------------
 template <int N> MT_HD f4v tex3_u8(const uint32_t* __restrict__ vol, f3 s) {
     constexpr unsigned M = (unsigned)N - 1u;
@@ -152,13 +198,14 @@ template <int N> MT_HD f4v tex3_u8(const uint32_t* __restrict__ vol, f3 s) {
     uint32_t t010 = __ldg(p0 + y1 * N + x0), t110 = __ldg(p0 + y1 * N + x1);
     uint32_t t001 = __ldg(p1 + y0 * N + x0), t101 = __ldg(p1 + y0 * N + x1);
     uint32_t t011 = __ldg(p1 + y1 * N + x0), t111 = __ldg(p1 + y1 * N + x1);
-    f4v c00 = lerp_texels(t000, t100, a);
-    f4v c10 = lerp_texels(t010, t110, a);
-    f4v c01 = lerp_texels(t001, t101, a);
-    f4v c11 = lerp_texels(t011, t111, a);
-    f4v c0 = lerp4(c00, c10, b);
-    f4v c1 = lerp4(c01, c11, b);
-    return lerp4(c0, c1, g) * (1.0f / 255.0f);
+    const float2 a2 = splat2(a), b2 = splat2(b), g2 = splat2(g);
+    const f4p c00 = lerp_texels(t000, t100, a2);
+    const f4p c10 = lerp_texels(t010, t110, a2);
+    const f4p c01 = lerp_texels(t001, t101, a2);
+    const f4p c11 = lerp_texels(t011, t111, a2);
+    const f4p c0 = lerp4p(c00, c10, b2);
+    const f4p c1 = lerp4p(c01, c11, b2);
+    return scale4p(lerp4p(c0, c1, g2), 1.0f / 255.0f);
 }
 
 template <int N> MT_HD f4v tex2_u8(const uint32_t* __restrict__ img, float sx, float sy) {
@@ -169,9 +216,10 @@ template <int N> MT_HD f4v tex2_u8(const uint32_t* __restrict__ img, float sx, f
     float a = u - fu, b = v - fv;
     unsigned iu = (unsigned)f2i(fu), iv = (unsigned)f2i(fv);
     unsigned x0 = iu & M, x1 = (iu + 1u) & M, y0 = iv & M, y1 = (iv + 1u) & M;
-    f4v c0 = lerp_texels(__ldg(img + y0 * N + x0), __ldg(img + y0 * N + x1), a);
-    f4v c1 = lerp_texels(__ldg(img + y1 * N + x0), __ldg(img + y1 * N + x1), a);
-    return lerp4(c0, c1, b) * (1.0f / 255.0f);
+    const float2 a2 = splat2(a);
+    const f4p c0 = lerp_texels(__ldg(img + y0 * N + x0), __ldg(img + y0 * N + x1), a2);
+    const f4p c1 = lerp_texels(__ldg(img + y1 * N + x0), __ldg(img + y1 * N + x1), a2);
+    return scale4p(lerp4p(c0, c1, splat2(b)), 1.0f / 255.0f);
 }
 
 // ---------------------------------------------------------------------------

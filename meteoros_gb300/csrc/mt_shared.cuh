@@ -172,8 +172,7 @@ MT_HD float relative_height(const Frame& F, f3 point, f3 ec, float lenInner, f3 
 
 // cloudRayMarch.comp:188-191
 MT_HD f3 relative_position(const Frame& F, f3 pos, f3 ec) {
-    const f3 d = pos - f3{ec.x, F.inner_alt, ec.z};
-    return f3{rdiv(d.x, F.r_thick), rdiv(d.y, F.r_thick), rdiv(d.z, F.r_thick)};
+    return rdiv3(pos - f3{ec.x, F.inner_alt, ec.z}, F.r_thick);
 }
 
 // cloudRayMarch.comp:475-487
