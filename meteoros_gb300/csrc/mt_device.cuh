@@ -154,6 +154,20 @@ struct f4p {
     float2 xy, zw;
 };
 MT_HD f4p lerp4p(f4p p, f4p q, float2 t) { return f4p{lerp2(p.xy, q.xy, t), lerp2(p.zw, q.zw, t)}; }
+MT_HD f4p pack4(f4v v) { return f4p{make_float2(v.x, v.y), make_float2(v.z, v.w)}; }
+MT_HD f4v unpack4(f4p v) { return f4v{v.xy.x, v.xy.y, v.zw.x, v.zw.y}; }
+MT_HD f4p add4p(f4p a, f4p b) { return f4p{add2(a.xy, b.xy), add2(a.zw, b.zw)}; }
+MT_HD f4p mul4p(f4p a, float s) { return f4p{mul2(a.xy, splat2(s)), mul2(a.zw, splat2(s))}; }
+// rdiv of four values by one denominator (rdiv_core on packed pairs: fma(q0, -b, a)
+// is fma(-q0, b, a) exactly), one range check; exceptional values redone one by one.
+MT_HD f4p rdiv4p(f4p a, Rcp r) {
+    const float2 y2 = splat2(r.y), nb2 = splat2(-r.b);
+    const float2 q0a = mul2(a.xy, y2), q0b = mul2(a.zw, y2);
+    const float2 qa = __ffma2_rn(__ffma2_rn(q0a, nb2, a.xy), y2, q0a);
+    const float2 qb = __ffma2_rn(__ffma2_rn(q0b, nb2, a.zw), y2, q0b);
+    if (rdiv_in_range(qa.x) & rdiv_in_range(qa.y) & rdiv_in_range(qb.x) & rdiv_in_range(qb.y)) return f4p{qa, qb};
+    return f4p{make_float2(rdiv(a.xy.x, r), rdiv(a.xy.y, r)), make_float2(rdiv(a.zw.x, r), rdiv(a.zw.y, r))};
+}
 MT_HD f4v scale4p(f4p c, float s) {
     const float2 xy = mul2(c.xy, splat2(s)), zw = mul2(c.zw, splat2(s));
     return f4v{xy.x, xy.y, zw.x, zw.y};

@@ -98,9 +98,23 @@ MT_HD void txaa_centre(const ViewConsts& v, int x, int y, int W, int H, float& i
     ppy = imin(imax(f2i(roundf((float)H * iuy)), 0), H - 1);
 }
 
+// A value the TXAA fast path accepts: non-negative and not NaN (+0 up to +inf).
+MT_HD bool txaa_plain(float4 c) {
+    const unsigned lim = 0x7f800000u;
+    return (__float_as_uint(c.x) <= lim) & (__float_as_uint(c.y) <= lim) & (__float_as_uint(c.z) <= lim) &
+           (__float_as_uint(c.w) <= lim);
+}
+MT_HD f4v fmin4(f4v a, f4v b) { return f4v{fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z), fminf(a.w, b.w)}; }
+MT_HD f4v fmax4(f4v a, f4v b) { return f4v{fmaxf(a.x, b.x), fmaxf(a.y, b.y), fmaxf(a.z, b.z), fmaxf(a.w, b.w)}; }
+
 // postProcess_TXAA.frag:223-269 for fragment (x, y); `load(i, j)` reads the
-// current frame (0 outside the image, as imageLoad does).
-template <class Load>
+// current frame (0 outside the image, as imageLoad does).  PLAIN: every value
+// `load` can return is non-negative and not NaN (txaa_plain).  Then the
+// neighbourhood minimum and maximum are the same value whatever the order of
+// comparison (equal non-negative floats have equal bits), so min/max
+// instructions over shared partial results replace the shader's nested
+// compare-selects, bit for bit.
+template <bool PLAIN, class Load>
 MT_HD f4v txaa_resolve(const mt_params& p, const ViewConsts& v, f4v prev, int x, int y, int W, int H, Load load) {
     float iux, iuy;
     int ppx, ppy;
@@ -108,18 +122,29 @@ MT_HD f4v txaa_resolve(const mt_params& p, const ViewConsts& v, f4v prev, int x,
     f4v ctl = load(ppx - 1, ppy - 1), ctc = load(ppx, ppy - 1), ctr = load(ppx + 1, ppy - 1);
     f4v cml = load(ppx - 1, ppy), cmc = load(ppx, ppy), cmr = load(ppx + 1, ppy);
     f4v cbl = load(ppx - 1, ppy + 1), cbc = load(ppx, ppy + 1), cbr = load(ppx + 1, ppy + 1);
-    f4v cmin = min4(ctl, min4(ctc, min4(ctr, min4(cml, min4(cmc, min4(cmr, min4(cbl, min4(cbc, cbr))))))));
-    f4v cmax = max4(ctl, max4(ctc, max4(ctr, max4(cml, max4(cmc, max4(cmr, max4(cbl, max4(cbc, cbr))))))));
-    const f4v s9 = ctl + ctc + ctr + cml + cmc + cmr + cbl + cbc + cbr;
+    f4v cmin, cmax, cmin5, cmax5;
+    if (PLAIN) {
+        cmin5 = fmin4(fmin4(fmin4(ctc, cml), fmin4(cmc, cmr)), cbc);
+        cmax5 = fmax4(fmax4(fmax4(ctc, cml), fmax4(cmc, cmr)), cbc);
+        cmin = fmin4(cmin5, fmin4(fmin4(ctl, ctr), fmin4(cbl, cbr)));
+        cmax = fmax4(cmax5, fmax4(fmax4(ctl, ctr), fmax4(cbl, cbr)));
+    } else {
+        cmin = min4(ctl, min4(ctc, min4(ctr, min4(cml, min4(cmc, min4(cmr, min4(cbl, min4(cbc, cbr))))))));
+        cmax = max4(ctl, max4(ctc, max4(ctr, max4(cml, max4(cmc, max4(cmr, max4(cbl, max4(cbc, cbr))))))));
+        cmin5 = min4(ctc, min4(cml, min4(cmc, min4(cmr, cbc))));
+        cmax5 = max4(ctc, max4(cml, max4(cmc, max4(cmr, cbc))));
+    }
+    // sums left to right as the shader adds them, channels in packed pairs
+    const f4p pctc = pack4(ctc), pcml = pack4(cml), pcmc = pack4(cmc), pcmr = pack4(cmr), pcbc = pack4(cbc);
+    const f4p s9 = add4p(add4p(add4p(add4p(add4p(add4p(add4p(add4p(pack4(ctl), pctc), pack4(ctr)), pcml), pcmc), pcmr),
+                                     pack4(cbl)), pcbc), pack4(cbr));
+    const f4p s5 = add4p(add4p(add4p(add4p(pctc, pcml), pcmc), pcmr), pcbc);
     const Rcp r9 = MT_RCP(0.0f, 9.0f), r5 = MT_RCP(0.0f, 5.0f);
-    f4v cavg = f4v{rdiv(s9.x, r9), rdiv(s9.y, r9), rdiv(s9.z, r9), rdiv(s9.w, r9)};
-    f4v cmin5 = min4(ctc, min4(cml, min4(cmc, min4(cmr, cbc))));
-    f4v cmax5 = max4(ctc, max4(cml, max4(cmc, max4(cmr, cbc))));
-    const f4v s5 = ctc + cml + cmc + cmr + cbc;
-    f4v cavg5 = f4v{rdiv(s5.x, r5), rdiv(s5.y, r5), rdiv(s5.z, r5), rdiv(s5.w, r5)};
-    cmin = f4v{0.5f * (cmin.x + cmin5.x), 0.5f * (cmin.y + cmin5.y), 0.5f * (cmin.z + cmin5.z), 0.5f * (cmin.w + cmin5.w)};
-    cmax = f4v{0.5f * (cmax.x + cmax5.x), 0.5f * (cmax.y + cmax5.y), 0.5f * (cmax.z + cmax5.z), 0.5f * (cmax.w + cmax5.w)};
-    cavg = f4v{0.5f * (cavg.x + cavg5.x), 0.5f * (cavg.y + cavg5.y), 0.5f * (cavg.z + cavg5.z), 0.5f * (cavg.w + cavg5.w)};
+    const f4p cavg9 = rdiv4p(s9, r9), cavg5 = rdiv4p(s5, r5);
+    // 0.5 * (a + b) per channel
+    cmin = unpack4(mul4p(add4p(pack4(cmin), pack4(cmin5)), 0.5f));
+    cmax = unpack4(mul4p(add4p(pack4(cmax), pack4(cmax5)), 0.5f));
+    const f4v cavg = unpack4(mul4p(add4p(cavg9, cavg5), 0.5f));
     f4v curr = cmc;
     // clip_aabb (:171-191)
     f4v pc = min4(max4(cavg, cmin), cmax);
@@ -140,7 +165,8 @@ MT_HD f4v txaa_resolve(const mt_params& p, const ViewConsts& v, f4v prev, int x,
     float ud = fabsf(lum0 - lum1) / gmax(lum0, gmax(lum1, 0.2f));
     float uw = 1.0f - ud;
     float k = gmix(p.feedback_min, p.feedback_max, uw * uw);
-    return mix4(prev, curr, k);
+    // mix(prev, curr, k) = prev * (1 - k) + curr * k per channel
+    return unpack4(add4p(mul4p(pack4(prev), 1.0f - k), mul4p(pack4(curr), k)));
 }
 
 // The history tap of fragment (x, y): the previous resolved frame sampled at
@@ -155,10 +181,10 @@ MT_HD f4v txaa_history(const ViewConsts& v, const float4* __restrict__ history, 
     return tex2_border(history, W, H, old_u, old_v);
 }
 
-template <class Load>
+template <bool PLAIN, class Load>
 MT_HD f4v txaa_pixel(const mt_params& p, const ViewConsts& v, const float4* __restrict__ history, int x, int y, int W,
                      int H, Load load) {
-    return txaa_resolve(p, v, txaa_history(v, history, x, y, W, H), x, y, W, H, load);
+    return txaa_resolve<PLAIN>(p, v, txaa_history(v, history, x, y, W, H), x, y, W, H, load);
 }
 
 // reprojection.comp:193-244 for every pixel the march does not write.
@@ -196,34 +222,41 @@ __global__ void __launch_bounds__(kTxaaTW * kTxaaTH) txaa_history_kernel(const _
 
 // HISTORY_IN_OUT: the history taps were stored in `out` by txaa_history_kernel.
 template <bool HISTORY_IN_OUT>
-__global__ void __launch_bounds__(kTxaaTW * kTxaaTH) txaa_kernel(const __grid_constant__ TxaaArgs a) {
+__global__ void __launch_bounds__(kTxaaTW * kTxaaTH, 4) txaa_kernel(const __grid_constant__ TxaaArgs a) {
     constexpr int SW = kTxaaTW + 3, SH = kTxaaTH + 3;
     __shared__ float4 tile[SH][SW];
     const int W = a.width, H = a.height;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
     const int x0 = blockIdx.x * kTxaaTW - 1, y0 = blockIdx.y * kTxaaTH - 1;
+    const int x = blockIdx.x * kTxaaTW + threadIdx.x, y = blockIdx.y * kTxaaTH + threadIdx.y;
+    const bool inside = x < W && y < H;
+    const size_t o = (size_t)y * (size_t)W + (size_t)x;
+    // the stored history tap, read before the tile so that the two loads overlap
+    float4 h = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (HISTORY_IN_OUT && inside) h = a.out[o];
+    bool plain = true;
     for (int i = tid; i < SW * SH; i += kTxaaTW * kTxaaTH) {
         const int gx = x0 + i % SW, gy = y0 + i / SW;
-        tile[i / SW][i % SW] = (gx >= 0 && gy >= 0 && gx < W && gy < H)
-                                   ? __ldg(a.current + (size_t)gy * (size_t)W + (size_t)gx)
-                                   : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        const float4 c = (gx >= 0 && gy >= 0 && gx < W && gy < H) ? __ldg(a.current + (size_t)gy * (size_t)W + (size_t)gx)
+                                                                  : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        plain = plain & txaa_plain(c);
+        tile[i / SW][i % SW] = c;
     }
-    __syncthreads();
-    const int x = blockIdx.x * kTxaaTW + threadIdx.x, y = blockIdx.y * kTxaaTH + threadIdx.y;
-    if (x >= W || y >= H) return;
+    // the whole tile non-negative and NaN-free: the block takes the min/max path
+    plain = __syncthreads_and(plain) != 0;
+    if (!inside) return;
     auto load = [&](int i, int j) -> f4v {
         const float4 s = tile[j - y0][i - x0];
         return f4v{s.x, s.y, s.z, s.w};
     };
-    const size_t o = (size_t)y * (size_t)W + (size_t)x;
     f4v prev;
     if (HISTORY_IN_OUT) {
-        const float4 h = a.out[o];
         prev = f4v{h.x, h.y, h.z, h.w};
     } else {
         prev = txaa_history(a.vc, a.history, x, y, W, H);
     }
-    const f4v r = txaa_resolve(a.params, a.vc, prev, x, y, W, H, load);
+    const f4v r = plain ? txaa_resolve<true>(a.params, a.vc, prev, x, y, W, H, load)
+                        : txaa_resolve<false>(a.params, a.vc, prev, x, y, W, H, load);
     a.out[o] = make_float4(r.x, r.y, r.z, r.w);
 }
 
@@ -243,6 +276,7 @@ __global__ void __launch_bounds__(TW * TH) resolve_kernel(const __grid_constant_
     const int x0 = blockIdx.x * TW - 1, y0 = blockIdx.y * TH - 1;
     const bool full = (a.flags & MT_RENDER_FULL) != 0;
     unsigned reprojected = 0;
+    bool plain = true;
     for (int i = threadIdx.x; i < SW * SH; i += TW * TH) {
         const int sx = i % SW, sy = i / SW;
         const int x = x0 + sx, y = y0 + sy;
@@ -261,9 +295,11 @@ __global__ void __launch_bounds__(TW * TH) resolve_kernel(const __grid_constant_
                 }
             }
         }
-        tile[sy][sx] = make_float4(v.x, v.y, v.z, v.w);
+        const float4 c = make_float4(v.x, v.y, v.z, v.w);
+        plain = plain & txaa_plain(c);
+        tile[sy][sx] = c;
     }
-    __syncthreads();
+    plain = __syncthreads_and(plain) != 0;
     const int tx = threadIdx.x % TW, ty = threadIdx.x / TW;
     const int x = x0 + 1 + tx, y = y0 + 1 + ty;
     if (x < W && y < H) {
@@ -272,7 +308,8 @@ __global__ void __launch_bounds__(TW * TH) resolve_kernel(const __grid_constant_
             const float4 s = tile[j - y0][i - x0];
             return f4v{s.x, s.y, s.z, s.w};
         };
-        const f4v r = txaa_pixel(a.params, a.vc_txaa, a.history, x, y, W, H, load);
+        const f4v r = plain ? txaa_pixel<true>(a.params, a.vc_txaa, a.history, x, y, W, H, load)
+                            : txaa_pixel<false>(a.params, a.vc_txaa, a.history, x, y, W, H, load);
         a.out[(size_t)y * (size_t)W + (size_t)x] = make_float4(r.x, r.y, r.z, r.w);
     }
     if (a.stats) {

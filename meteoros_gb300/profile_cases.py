@@ -6,6 +6,8 @@ time under a profiler (a few launches, a few hundred MB on the device).
 cases:
   march_full      960x540 full-raymarch frame (march_kernel<1>), config 0 view
   march_cb        1920x1080 checkerboard frame (march_kernel<4> + reprojection)
+  frame           1920x1080 reprojected frame through mt_render_frame (raymarch, reprojection
+                  and TXAA history beside it, then the TXAA resolve)
   txaa            1920x1080 TXAA resolve
   batch           64-view batched raymarch (march_batch_kernel), RGBA8 volumes
   batch_fp16      the same with FP16 volumes
@@ -55,6 +57,16 @@ def main(argv=None) -> int:
                 ctx.render(cam, old, tm, params, prev, cur, None, abi.MT_RENDER_CHECKERBOARD)
             else:
                 ctx.txaa(cam, old, tm, params, prev, cur, out)
+    elif a.case == "frame":
+        W, H = 1920, 1080
+        seq = scenes.config_sequence(SEED, W, H, frames=a.reps)
+        prev = torch.rand((H, W, 4), device=dev)
+        hist = torch.rand((H, W, 4), device=dev)
+        cur = torch.zeros_like(prev)
+        out = torch.zeros_like(prev)
+        mask = torch.zeros((H, W), device=dev)
+        for cam, old, tm, params in seq:
+            ctx.render_frame(cam, old, tm, params, prev, cur, hist, out, mask)
     elif a.case in ("batch", "batch_fp16"):
         storage = abi.MT_STORAGE_F16 if a.case == "batch_fp16" else abi.MT_STORAGE_U8
         specs = scenes.config3_views(SEED, n_views=64)

@@ -115,7 +115,8 @@ class Context:
 
     def render_frame(self, camera, camera_old, time, params, prev, cur, history, out, mask=None,
                      flags: int = abi.MT_RENDER_CHECKERBOARD, stream=None) -> None:
-        """Raymarch + reprojection + TXAA of one frame in two launches."""
+        """Raymarch, reprojection and TXAA of one frame: the reprojection and the
+        TXAA history taps run beside the raymarch, the TXAA resolve after it."""
         h, w = int(cur.shape[0]), int(cur.shape[1])
         self._check(self.lib.mt_render_frame(self.handle, C.byref(camera), C.byref(camera_old), C.byref(time),
                                              C.byref(params), _ptr(prev), _ptr(cur), _ptr(history), _ptr(out),

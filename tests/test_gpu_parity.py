@@ -122,6 +122,27 @@ def test_dispatch_quirk_against_golden(ref_ctx, golden):
     assert np.isnan(gm[:, 128:]).all()
 
 
+def test_txaa_signed_and_special_values_bit_exact(ctx, oracle, golden):
+    """Blocks whose neighbourhoods hold negative values, -0, NaN or infinity
+    take the compare-select path of the resolve, the others the min/max path:
+    both equal the oracle bit for bit."""
+    _, _, _, cur, hist = mg.txaa_inputs()
+    cam, old, tm = mg.ubos_from(golden["txaa_ubo"], abi.CameraUBO, abi.CameraUBO, abi.TimeUBO)
+    cur = cur.copy()
+    h, w = cur.shape[:2]
+    rng = np.random.default_rng(17)
+    n = max(8, (h * w) // 500)
+    ys, xs = rng.integers(0, h, n), rng.integers(0, w, n)
+    special = np.array([-0.0, -1.5, -1e-30, np.inf, np.nan, 0.0], np.float32)
+    cur[ys, xs, rng.integers(0, 4, n)] = special[rng.integers(0, len(special), n)]
+    cur[: h // 3, : w // 3] *= -1.0  # a negative region
+    for params in (abi.params_reference(), abi.params_config()):
+        want = oracle.txaa(cam, old, tm, params, cur, hist)
+        out = torch.zeros_like(to_dev(cur, torch))
+        ctx.txaa(cam, old, tm, params, to_dev(cur, torch), to_dev(hist, torch), out)
+        assert_bits_equal(out.cpu().numpy(), want, "txaa with special values")
+
+
 def test_txaa_bit_exact(ctx, oracle, golden):
     _, _, _, cur, hist = mg.txaa_inputs()
     cam, old, tm = mg.ubos_from(golden["txaa_ubo"], abi.CameraUBO, abi.CameraUBO, abi.TimeUBO)
