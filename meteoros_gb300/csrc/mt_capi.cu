@@ -211,6 +211,7 @@ mt_status build_march_args(mt_ctx* ctx, const mt_camera_ubo* cam, const mt_camer
     mt::make_view_consts(&a->vc_repro, *p, *cam, *cam_old, *tm, w, h, true);
     mt::make_view_consts(&a->vc_txaa, *p, *cam, *cam_old, *tm, w, h, false);
     mt::make_march_jitter(a->jitter, *tm);
+    mt::make_march_frame(&a->frame, *p, *cam, *tm);
     a->bottom_up = ctx->march_order == 0 ? 1 : 0;
     a->lanes = ctx->march_lanes;
     if (a->lanes == 0) {

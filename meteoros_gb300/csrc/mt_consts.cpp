@@ -83,4 +83,23 @@ void make_march_jitter(float out[16][3], const mt_time_ubo& tm) {
     }
 }
 
+void make_march_frame(Frame* f, const mt_params& p, const mt_camera_ubo& cam, const mt_time_ubo& tm) {
+    f->R = p.earth_radius;
+    f->Rin = p.shell_inner_radius;
+    f->Rout = p.shell_outer_radius;
+    f->thickness = f->Rout - f->Rin;
+    f->inner_alt = f->Rin - f->R;
+    f->r_thick = Rcp{f->thickness, 1.0f / f->thickness};
+    f->r_period = Rcp{p.noise_period, 1.0f / p.noise_period};
+    f->r_weather = Rcp{p.weather_scale, 1.0f / p.weather_scale};
+    for (int i = 0; i < 3; ++i) {
+        f->eye[i] = p.eye_sign * cam.eye[i];
+        f->wind_t[i] = (p.wind_dir[i] * p.wind_speed) * tm.time[1];
+        f->skew[i] = p.skew_dir[i];
+    }
+    f->ec[0] = f->eye[0];
+    f->ec[1] = -f->R;
+    f->ec[2] = f->eye[2];
+}
+
 }  // namespace mt

@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/meteoros.h"
+#include "mt_kernels.h"
 
 #define MT_HD __device__ __forceinline__
 
@@ -70,9 +71,6 @@ MT_HD int f2i(float v) { return __float2int_rz(v); }
 // quotients go through the IEEE division; a zero dividend takes q0, which
 // carries the quotient's sign when y is finite.
 // ---------------------------------------------------------------------------
-struct Rcp {
-    float b, y;
-};
 // The IEEE division, out of line: one shared copy keeps the callers small in
 // the instruction cache (the march loop is instruction-fetch bound otherwise).
 static __device__ __noinline__ float div_ieee(float a, float b) { return a / b; }

@@ -27,6 +27,26 @@ struct ViewConsts {
 void make_view_consts(ViewConsts* v, const mt_params& p, const mt_camera_ubo& cam, const mt_camera_ubo& cam_old,
                       const mt_time_ubo& tm, int W, int H, bool repro);
 
+// A denominator b and its correctly rounded reciprocal y = RN(1/b) (see rdiv).
+struct Rcp {
+    float b, y;
+};
+
+// The per-frame constants of the raymarch (cloudRayMarch.comp:565-688 and the
+// helpers it calls), computed on the host (mt_consts.cpp) with the shader's
+// IEEE FP32 operations: kept in the kernel's parameter space, they take no
+// registers in the march loop.
+struct Frame {
+    float R, Rin, Rout, thickness, inner_alt;  // earth radius, shell radii, Rout - Rin, Rin - R
+    Rcp r_thick, r_period, r_weather;          // thickness, noise_period, weather_scale
+    float eye[3];                              // ray origin: eye_sign * camera eye
+    float ec[3];                               // earth centre (eye.x, -R, eye.z)
+    float wind_t[3];                           // (wind_dir * wind_speed) * time[1]
+    float skew[3];                             // skew_dir
+};
+
+void make_march_frame(Frame* f, const mt_params& p, const mt_camera_ubo& cam, const mt_time_ubo& tm);
+
 struct MarchArgs {
     mt_camera_ubo camera;
     mt_camera_ubo camera_old;
@@ -60,6 +80,7 @@ struct MarchArgs {
     // the 16 values of its index: jx = halton / 1 / 75, jy likewise, and
     // (jx + jy) * 1.18, evaluated on the host in that order (make_march_jitter).
     float jitter[16][3];
+    Frame frame;
 };
 
 void make_march_jitter(float out[16][3], const mt_time_ubo& tm);

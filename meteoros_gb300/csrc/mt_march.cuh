@@ -90,26 +90,21 @@ template <int S> MT_HD float erosion_modifier(const Tex<S>& tx, f3 point, float 
     float hfbm = (hf.x * 0.625f) + (hf.y * 0.25f) + (hf.z * 0.125f);
     return gclamp(gmix(hfbm, 1.0f - hfbm, gclamp(h * 2.0f, 0.0f, 1.0f)), 0.0f, 1.0f);
 }
-// Per-ray constants of cloudRayMarch.comp:565-624, shared by every step.
+// Per-ray constants of cloudRayMarch.comp:565-624, shared by every step (the
+// per-frame ones are in Frame).
 struct RayConsts {
-    Ray ray;
-    f3 ec, startPos;
+    f3 dir, startPos;
     f3 koff[6];  // cone-light offsets: (stepSize * kernel[i]) * i
-    f3 wind_t, skew;  // wind * total time
     float stepSize, cos_angle, cos_q, HG_light, lenInner;
-    int pixelID;
-    const float (*jitter)[3];  // per jitter index: (jx, (jx + jy) * 1.18, jy), see MarchArgs::jitter
 };
 
-static __device__ __noinline__ void ray_consts(const mt_params& p, const mt_time_ubo& tm, const Ray& ray, f3 ec,
-                                        f3 startPos, float stepSize, int pixelID, RayConsts& rc) {
-    rc.ray = ray;
-    rc.ec = ec;
+static __device__ __noinline__ void ray_consts(const mt_params& p, const Frame& F, f3 dir, f3 startPos,
+                                               float stepSize, RayConsts& rc) {
+    rc.dir = dir;
     rc.startPos = startPos;
     rc.stepSize = stepSize;
-    rc.pixelID = pixelID;
-    const f3 lightDir = normalize3(ld3(p.sun_light_pos) - ray.origin);
-    rc.cos_angle = dot3(normalize3(ray.direction), lightDir);
+    const f3 lightDir = normalize3(ld3(p.sun_light_pos) - ld3(F.eye));
+    rc.cos_angle = dot3(normalize3(dir), lightDir);
     rc.cos_q = (rc.cos_angle - 0.7f) / (1.0f - 0.7f);
     rc.HG_light = gmax(henyey_greenstein(rc.cos_angle, 0.6f), 0.7f * henyey_greenstein(rc.cos_angle, 0.99f - 0.1f));
     float ax = fabsf(lightDir.x), ay = fabsf(lightDir.y), az = fabsf(lightDir.z);
@@ -131,9 +126,7 @@ static __device__ __noinline__ void ray_consts(const mt_params& p, const mt_time
     // the step-independent part of the light sample position
     // pos + ((stepSize * kernel[i]) * i) (cloudRayMarch.comp:656)
     for (int i = 0; i < 6; ++i) rc.koff[i] = (stepSize * kernel[i]) * (float)i;
-    rc.wind_t = (ld3(p.wind_dir) * p.wind_speed) * tm.time[1];
-    rc.lenInner = length3(startPos - ray.origin);
-    rc.skew = ld3(p.skew_dir);
+    rc.lenInner = length3(startPos - ld3(F.eye));
 }
 
 struct StepOut {
@@ -147,18 +140,18 @@ struct StepOut {
 // running accumDensity / transmittance.
 template <int S>
 MT_HD StepOut eval_step(const mt_params& p, const Frame& F, const Tex<S>& tx, const mt_time_ubo& tm,
-                        const RayConsts& rc, float t) {
+                        const float (*jitter)[3], const RayConsts& rc, float t) {
     StepOut o{0, 0.0f, 0.0f};
-    const int _index = f2i(gmod((float)(rc.pixelID + f2i(t)), 16.0f));
-    const float* j = rc.jitter[_index & 15];  // _index is in 0..15 for every finite t
-    f3 jd = rc.ray.direction + f3{j[0], j[1], j[2]};
-    f3 pos = rc.ray.origin + t * jd;
-    f3 sp = relative_position(F, pos, rc.ec);
+    const int _index = f2i(gmod((float)(tm.frame_count_mod16 + f2i(t)), 16.0f));
+    const float* j = jitter[_index & 15];  // _index is in 0..15 for every finite t
+    f3 jd = rc.dir + f3{j[0], j[1], j[2]};
+    f3 pos = ld3(F.eye) + t * jd;
+    f3 sp = relative_position(F, pos, ld3(F.ec));
     sp = f3{rdiv(sp.x, F.r_period), rdiv(sp.y, F.r_period), rdiv(sp.z, F.r_period)};
-    float relH = relative_height(F, pos, rc.ec, rc.lenInner, rc.ray.direction, rc.ray.origin);
-    sp = sp + ((relH * rc.skew) * p.cloud_top_offset) * 0.009f;
-    sp = sp + rc.wind_t;
-    Weather wt = weather_at<S>(p, F, tx, pos, rc.ec);
+    float relH = relative_height(F, pos, ld3(F.ec), rc.lenInner, rc.dir, ld3(F.eye));
+    sp = sp + ((relH * ld3(F.skew)) * p.cloud_top_offset) * 0.009f;
+    sp = sp + ld3(F.wind_t);
+    Weather wt = weather_at<S>(p, F, tx, pos, ld3(F.ec));
     if (p.height_gradient) wt.hgrad = height_gradient(relH, wt.type);
     // A zero height gradient or zero coverage makes the density 0 (or NaN
     // when the coverage is 0), never > 0: the step is empty whatever the base
@@ -175,7 +168,7 @@ MT_HD StepOut eval_step(const mt_params& p, const Frame& F, const Tex<S>& tx, co
 #pragma unroll 1
         for (int i = 0; i < 6; ++i) {
             f3 lightPos = pos + rc.koff[i];
-            f3 slp = relative_position(F, lightPos, rc.ec);
+            f3 slp = relative_position(F, lightPos, ld3(F.ec));
             float cbl = sample_low_frequency<S>(p, tx, slp, relH, wt);
             if (cbl > 0.0f) dl = dl + erode(1.5f * cbl, ero);
         }
@@ -193,9 +186,9 @@ MT_HD StepOut eval_step(const mt_params& p, const Frame& F, const Tex<S>& tx, co
 // the sequential loop's.
 template <int G, int S>
 MT_HD f3 ray_march_group(const mt_params& p, const Frame& F, const Tex<S>& tx, const mt_time_ubo& tm,
-                         const float (*jitter)[3], const Ray& ray, f3 ec, f3 startPos, float start_t, float end_t,
-                         int pixelID, float& accum, Counts& cnt, unsigned gmask, int lane) {
-    float _dot = dot3(ray.direction, f3{0.0f, 1.0f, 0.0f});
+                         const float (*jitter)[3], f3 dir, f3 startPos, float start_t, float end_t, float& accum,
+                         Counts& cnt, unsigned gmask, int lane) {
+    float _dot = dot3(dir, f3{0.0f, 1.0f, 0.0f});
     float maxSteps;
     if (p.steps_min == p.steps_max)
         maxSteps = (float)p.steps_min;
@@ -204,8 +197,7 @@ MT_HD f3 ray_march_group(const mt_params& p, const Frame& F, const Tex<S>& tx, c
     const float thick = end_t - start_t;
     const float stepSize = thick / maxSteps;
     RayConsts rc;
-    ray_consts(p, tm, ray, ec, startPos, stepSize, pixelID, rc);
-    rc.jitter = jitter;
+    ray_consts(p, F, dir, startPos, stepSize, rc);
     float transmittance = 1.0f;
     f3 color{0.0f, 0.0f, 0.0f};
     // Iteration guard (not in the reference): a step below the ulp of t would
@@ -220,7 +212,7 @@ MT_HD f3 ray_march_group(const mt_params& p, const Frame& F, const Tex<S>& tx, c
         for (int k = 0; k < lane; ++k) t += stepSize;
         const int valid = (t < end_t) && (s_base + lane < cap);
         StepOut o{0, 0.0f, 0.0f};
-        if (valid) o = eval_step<S>(p, F, tx, tm, rc, t);
+        if (valid) o = eval_step<S>(p, F, tx, tm, jitter, rc, t);
 #pragma unroll
         for (int k = 0; k < G; ++k) {
             if (!__shfl_sync(gmask, valid, k, G)) {
@@ -261,8 +253,7 @@ MT_HD void march_pixel(const MarchArgs& a, const Frame& F, const Tex<S>& tx, int
     const int pixelID = a.time.frame_count_mod16;
     float ux = (float)px / (float)W, uy = (float)py / (float)H;
     uy = 1.0f - uy;
-    f3 eyePos = p.eye_sign * ld3(a.camera.eye);
-    Ray ray = cast_ray(ux, uy, eyePos, a.camera, a.time, pixelID, W, H, false);
+    Ray ray = cast_ray(ux, uy, ld3(F.eye), a.camera, a.time, pixelID, W, H, false);
     const float sunIntensity = 0.780f;
     float _dot = dot3(f3{0.0f, 1.0f, 0.0f}, ray.direction);
     const float bgMul = gmax(0.620f, _dot);
@@ -288,8 +279,7 @@ MT_HD void march_pixel(const MarchArgs& a, const Frame& F, const Tex<S>& tx, int
         }
         return;
     }
-    f3 ec = eyePos;
-    ec.y = -F.R;
+    const f3 ec = ld3(F.ec);
     Isect in, out;
     if (p.fp64_shells) {
         in = ray_sphere_fp64(ray.origin, ray.direction, ec, F.Rin);
@@ -299,8 +289,8 @@ MT_HD void march_pixel(const MarchArgs& a, const Frame& F, const Tex<S>& tx, int
         out = ray_sphere(ray.origin, ray.direction, ec, F.Rout);
     }
     float accum = 0.0f;
-    f3 res = ray_march_group<G, S>(p, F, tx, a.time, a.jitter, ray, ec, in.point, in.t, out.t, pixelID, accum, cnt,
-                                   gmask, lane);
+    f3 res = ray_march_group<G, S>(p, F, tx, a.time, a.jitter, ray.direction, in.point, in.t, out.t, accum, cnt, gmask,
+                                   lane);
     if (lane != 0) return;
     float godAccum = accum;
     accum = accum * gsmoothstep(0.0f, 1.0f, gmin(1.0f, remap(ray.direction.y, fade, 0.2f, 0.0f, 1.0f)));
@@ -317,7 +307,7 @@ MT_HD void march_pixel(const MarchArgs& a, const Frame& F, const Tex<S>& tx, int
 template <int G, int S, int BS>
 __global__ void __launch_bounds__(BS, 1024 / BS) march_kernel(const __grid_constant__ MarchArgs a) {
     static_assert(G >= 1 && G <= 32 && (32 % G) == 0, "G must divide the warp");
-    const Frame F = make_frame(a.params);
+    const Frame& F = a.frame;
     using T = typename Vol<S>::T;
     const Tex<S> tx{(const T*)a.vol[0], (const T*)a.vol[1], (const T*)a.vol[2], (const T*)a.vol[3]};
     const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -373,7 +363,7 @@ __global__ void __launch_bounds__(128, 8) march_batch_kernel(const __grid_consta
         if (t >= b.n_tiles) break;
         const BatchTile tile = b.tiles[t];
         const MarchArgs& a = b.views[tile.view];
-        const Frame F = make_frame(a.params);
+        const Frame& F = a.frame;
         const Tex<S> tx{(const T*)a.vol[0], (const T*)a.vol[1], (const T*)a.vol[2], (const T*)a.vol[3]};
         const bool full = (a.flags & MT_RENDER_FULL) != 0;
         const int id = a.time.frame_count_mod16;

@@ -9,24 +9,6 @@
 
 namespace mt {
 
-struct Frame {
-    float R, Rin, Rout, thickness, inner_alt;
-    Rcp r_thick, r_period, r_weather;  // per-frame denominators (see rdiv)
-};
-
-MT_HD Frame make_frame(const mt_params& p) {
-    Frame F;
-    F.R = p.earth_radius;
-    F.Rin = p.shell_inner_radius;
-    F.Rout = p.shell_outer_radius;
-    F.thickness = F.Rout - F.Rin;
-    F.inner_alt = F.Rin - F.R;
-    F.r_thick = make_rcp(F.thickness);
-    F.r_period = make_rcp(p.noise_period);
-    F.r_weather = make_rcp(p.weather_scale);
-    return F;
-}
-
 // remap() whose range width omax - omin is known ahead: the quotient through
 // the correctly rounded reciprocal of that width (rdiv).
 MT_HD float remap_r(float v, float omin, Rcp width, float nmin, float nmax) {
