@@ -98,8 +98,7 @@ struct RayConsts {
     float stepSize, cos_angle, cos_q, HG_light, lenInner;
 };
 
-static __device__ __noinline__ void ray_consts(const mt_params& p, const Frame& F, f3 dir, f3 startPos,
-                                               float stepSize, RayConsts& rc) {
+MT_HD void ray_consts(const mt_params& p, const Frame& F, f3 dir, f3 startPos, float stepSize, RayConsts& rc) {
     rc.dir = dir;
     rc.startPos = startPos;
     rc.stepSize = stepSize;
