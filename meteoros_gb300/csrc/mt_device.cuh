@@ -105,10 +105,7 @@ MT_HD float dot3(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 MT_HD float length3(f3 a) { return sqrtf(dot3(a, a)); }
 MT_HD f3 normalize3(f3 a) { return a / length3(a); }
 // normalize(v) = v / length(v), the three divisions sharing one reciprocal.
-MT_HD f3 normalize3_r(f3 a) {
-    const Rcp r = make_rcp(length3(a));
-    return f3{rdiv(a.x, r), rdiv(a.y, r), rdiv(a.z, r)};
-}
+MT_HD f3 normalize3_r(f3 a) { return rdiv3(a, make_rcp(length3(a))); }
 MT_HD f3 cross3(f3 a, f3 b) { return f3{a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y}; }
 MT_HD f3 mix3(f3 x, f3 y, float a) { return f3{gmix(x.x, y.x, a), gmix(x.y, y.y, a), gmix(x.z, y.z, a)}; }
 MT_HD f4v min4(f4v a, f4v b) { return f4v{gmin(a.x, b.x), gmin(a.y, b.y), gmin(a.z, b.z), gmin(a.w, b.w)}; }
@@ -306,14 +303,15 @@ MT_HD f4v tex2_border(const float4* __restrict__ img, int W, int H, float sx, fl
     float a = u - fu, b = v - fv;
     int i0 = f2i(fu), j0 = f2i(fv);
     long long i1 = (long long)i0 + 1, j1 = (long long)j0 + 1;
-    auto at = [&](long long i, long long j) -> f4v {
-        if (i < 0 || j < 0 || i >= W || j >= H) return f4v{0.0f, 0.0f, 0.0f, 1.0f};
+    auto at = [&](long long i, long long j) -> f4p {
+        if (i < 0 || j < 0 || i >= W || j >= H) return f4p{make_float2(0.0f, 0.0f), make_float2(0.0f, 1.0f)};
         float4 q = __ldg(img + (size_t)j * (size_t)W + (size_t)i);
-        return f4v{q.x, q.y, q.z, q.w};
+        return f4p{make_float2(q.x, q.y), make_float2(q.z, q.w)};
     };
-    f4v c0 = lerp4(at(i0, j0), at(i1, j0), a);
-    f4v c1 = lerp4(at(i0, j1), at(i1, j1), a);
-    return lerp4(c0, c1, b);
+    const float2 a2 = splat2(a);
+    const f4p c0 = lerp4p(at(i0, j0), at(i1, j0), a2);
+    const f4p c1 = lerp4p(at(i0, j1), at(i1, j1), a2);
+    return unpack4(lerp4p(c0, c1, splat2(b)));
 }
 
 }  // namespace mt

@@ -61,8 +61,7 @@ MT_HD void old_uv(const ViewConsts& v, float sx, float sy, float& old_u, float& 
     f3 od{ov[0] * q.x + ov[4] * q.y + ov[8] * q.z + ov[12] * 1.0f, ov[1] * q.x + ov[5] * q.y + ov[9] * q.z + ov[13] * 1.0f,
           ov[2] * q.x + ov[6] * q.y + ov[10] * q.z + ov[14] * 1.0f};
     od = normalize3_r(od);
-    const Rcp rz = make_rcp(-od.z);
-    od = f3{rdiv(od.x, rz), rdiv(od.y, rz), rdiv(od.z, rz)};
+    od = rdiv3(od, make_rcp(-od.z));
     old_u = rdiv(od.x, rcp_of(v.r_tanx)) * 0.5f + 0.5f;
     old_v = rdiv(od.y, rcp_of(v.r_tany)) * 0.5f + 0.5f;
 }
@@ -74,19 +73,19 @@ MT_HD f4v reproject_pixel(const MarchArgs& a, const ViewConsts& v, int x, int y)
     float old_u, old_v;
     old_uv(v, ux, uy, old_u, old_v);
     const float mx = old_u - ux, my = old_v - uy;
-    f4v blur{0.0f, 0.0f, 0.0f, 0.0f};
+    // (old - m * f) * (W, H) for u and v as one packed pair; the blur sum in pairs
+    const float2 o2 = make_float2(old_u, old_v), m2 = make_float2(mx, my), wh = make_float2((float)W, (float)H);
+    f4p blur{make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f)};
 #pragma unroll
     for (int i = 0; i < 10; ++i) {
         const float f = (float)i / 10.0f;
-        const float iu = roundf((old_u - mx * f) * (float)W);
-        const float iv = roundf((old_v - my * f) * (float)H);
-        const int ix = imin(imax(f2i(iu), 0), W - 1);
-        const int iy = imin(imax(f2i(iv), 0), H - 1);
+        const float2 q = mul2(sub2(o2, mul2(m2, splat2(f))), wh);
+        const int ix = imin(imax(f2i(roundf(q.x)), 0), W - 1);
+        const int iy = imin(imax(f2i(roundf(q.y)), 0), H - 1);
         const float4 s = __ldg(a.prev + (size_t)iy * (size_t)W + (size_t)ix);
-        blur = blur + f4v{s.x, s.y, s.z, s.w};
+        blur = add4p(blur, f4p{make_float2(s.x, s.y), make_float2(s.z, s.w)});
     }
-    const Rcp r10 = MT_RCP(0.0f, 10.0f);
-    return f4v{rdiv(blur.x, r10), rdiv(blur.y, r10), rdiv(blur.z, r10), rdiv(blur.w, r10)};
+    return unpack4(rdiv4p(blur, MT_RCP(0.0f, 10.0f)));
 }
 
 // The centre pixel of fragment (x, y)'s neighbourhood: pixelPos of
