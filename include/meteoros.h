@@ -167,7 +167,7 @@ typedef struct mt_tuning {
     int32_t reproject_serial; /* mt_render / mt_render_frame, checkerboard: 0 = the reprojection
                                * runs on a second stream beside the raymarch (default; the call
                                * still completes in `stream` order); 1 = before it on `stream` */
-    int32_t march_block;   /* mt_render: raymarch CTA size, 32 or 128 threads; 0 = default (128) */
+    int32_t march_block;   /* mt_render: raymarch CTA size, 32, 128 or 256 threads; 0 = default (256) */
     int32_t march_order;   /* mt_render / mt_render_batch: 0 = ray rows dispatched bottom to top
                             * (default: the rows below the horizon, which do not march, first,
                             * then the marching rows from the horizon up); 1 = top to bottom */

@@ -38,7 +38,7 @@ struct mt_ctx {
     cudaEvent_t ev[8] = {};                   // reproject, march, txaa, resolve (start, end)
     bool ran[4] = {false, false, false, false};
     int march_lanes = 0;                      // step-parallel lanes per ray (mt_set_tuning); 0 = auto
-    int march_block = 128;                    // march_kernel CTA size (mt_set_tuning)
+    int march_block = 256;                    // march_kernel CTA size (mt_set_tuning)
     int march_order = 0;                      // ray rows: 0 bottom to top, 1 top to bottom
     int fused_resolve = 0;                    // mt_render_frame: reprojection fused with TXAA
     // mt_render_batch
@@ -876,8 +876,8 @@ MT_API mt_status mt_set_tuning(mt_ctx* ctx, const mt_tuning* t) {
     if (t->batch_direct != 0 && t->batch_direct != 1) return fail(ctx, MT_ERR_INVALID_ARG, "batch_direct must be 0 or 1");
     if (t->reproject_serial != 0 && t->reproject_serial != 1)
         return fail(ctx, MT_ERR_INVALID_ARG, "reproject_serial must be 0 or 1");
-    if (t->march_block != 0 && t->march_block != 32 && t->march_block != 128)
-        return fail(ctx, MT_ERR_INVALID_ARG, "march_block must be 0 (default 128), 32 or 128");
+    if (t->march_block != 0 && t->march_block != 32 && t->march_block != 128 && t->march_block != 256)
+        return fail(ctx, MT_ERR_INVALID_ARG, "march_block must be 0 (default 256), 32, 128 or 256");
     if (t->march_order != 0 && t->march_order != 1) return fail(ctx, MT_ERR_INVALID_ARG, "march_order must be 0 or 1");
     ctx->march_lanes = t->march_lanes;
     ctx->fused_resolve = t->fused_resolve;
@@ -886,7 +886,7 @@ MT_API mt_status mt_set_tuning(mt_ctx* ctx, const mt_tuning* t) {
     ctx->batch_lanes = t->batch_lanes;
     ctx->batch_direct = t->batch_direct;
     ctx->overlap = t->reproject_serial ? 0 : 1;
-    ctx->march_block = t->march_block == 0 ? 128 : t->march_block;
+    ctx->march_block = t->march_block == 0 ? 256 : t->march_block;
     ctx->march_order = t->march_order;
     return MT_OK;
 }

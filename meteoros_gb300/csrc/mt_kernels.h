@@ -64,7 +64,7 @@ struct MarchArgs {
     int32_t groups_x, groups_y;  // 4x4 blocks covered by the reference's raymarch dispatch
     uint32_t flags;
     int32_t lanes;               // lanes marching one ray together: 1, 4, 8 or 16
-    int32_t block;               // march_kernel CTA size: 32 or 128 threads
+    int32_t block;               // march_kernel CTA size: 32, 128 or 256 threads
     // Dispatch order of the ray rows (rows of 4x4 blocks, or of pixels for a
     // full frame): 1 = bottom to top (default), 0 = top to bottom.  Bottom to
     // top runs the rows that do not march (below the fade elevation, 10-50x

@@ -301,8 +301,8 @@ MT_HD void march_pixel(const MarchArgs& a, const Frame& F, const Tex<S>& tx, int
 // Ray -> marched pixel.  Checkerboard: the reference's group grid covers
 // groups_x x groups_y blocks of 4x4 (Renderer.cpp:713-716); each ray is one
 // block's slot pixel.  Full: one ray per pixel.  G consecutive lanes (an
-// aligned segment of a warp) march one ray.  BS threads per CTA (128 by
-// default, 32 selectable), 64 registers a thread either way.
+// aligned segment of a warp) march one ray.  BS threads per CTA (256 by
+// default, 128 or 32 selectable), 64 registers a thread in every case.
 template <int G, int S, int BS>
 __global__ void __launch_bounds__(BS, 1024 / BS) march_kernel(const __grid_constant__ MarchArgs a) {
     static_assert(G >= 1 && G <= 32 && (32 % G) == 0, "G must divide the warp");
@@ -417,7 +417,9 @@ template <int S, int BS> void launch_march_bs(const MarchArgs& a, cudaStream_t s
 }
 
 template <int S> cudaError_t launch_march_storage(const MarchArgs& a, cudaStream_t s, long long rays) {
-    if (a.block == 128)
+    if (a.block == 256)
+        launch_march_bs<S, 256>(a, s, rays);
+    else if (a.block == 128)
         launch_march_bs<S, 128>(a, s, rays);
     else
         launch_march_bs<S, 32>(a, s, rays);

@@ -202,11 +202,11 @@ __global__ void __launch_bounds__(256) reproject_kernel(const __grid_constant__ 
     }
 }
 
-// postProcess_TXAA.frag:223-269, one thread per output pixel (fragment).
-// A 32x8 CTA stages the current frame over its pixels plus the halo the
-// neighbourhoods reach (the centre is the fragment's pixel or the next one:
-// one column/row before, two after) in shared memory, zero outside the image
-// as imageLoad returns; the nine taps per pixel then read shared memory.
+// postProcess_TXAA.frag:223-269 per output pixel (fragment).  A CTA stages
+// the current frame over its pixels plus the halo the neighbourhoods reach
+// (the centre is the fragment's pixel or the next one: one column/row before,
+// two after) in shared memory, zero outside the image as imageLoad returns;
+// the nine taps per pixel then read shared memory.
 constexpr int kTxaaTW = 32, kTxaaTH = 8;
 
 // The history taps of a frame, into `out` (which the resolve then reads back
@@ -219,20 +219,25 @@ __global__ void __launch_bounds__(kTxaaTW * kTxaaTH) txaa_history_kernel(const _
     a.out[(size_t)y * (size_t)a.width + (size_t)x] = make_float4(h.x, h.y, h.z, h.w);
 }
 
+// The resolve: a 32x8 CTA owns a 32x16 tile, each thread two pixels 8 rows
+// apart (the halo and the barrier are shared by twice the pixels).
 // HISTORY_IN_OUT: the history taps were stored in `out` by txaa_history_kernel.
+constexpr int kTxaaRows = 2;
 template <bool HISTORY_IN_OUT>
 __global__ void __launch_bounds__(kTxaaTW * kTxaaTH, 4) txaa_kernel(const __grid_constant__ TxaaArgs a) {
-    constexpr int SW = kTxaaTW + 3, SH = kTxaaTH + 3;
+    constexpr int TH = kTxaaTH * kTxaaRows, SW = kTxaaTW + 3, SH = TH + 3;
     __shared__ float4 tile[SH][SW];
     const int W = a.width, H = a.height;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-    const int x0 = blockIdx.x * kTxaaTW - 1, y0 = blockIdx.y * kTxaaTH - 1;
-    const int x = blockIdx.x * kTxaaTW + threadIdx.x, y = blockIdx.y * kTxaaTH + threadIdx.y;
-    const bool inside = x < W && y < H;
-    const size_t o = (size_t)y * (size_t)W + (size_t)x;
-    // the stored history tap, read before the tile so that the two loads overlap
-    float4 h = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    if (HISTORY_IN_OUT && inside) h = a.out[o];
+    const int x0 = blockIdx.x * kTxaaTW - 1, y0 = blockIdx.y * TH - 1;
+    const int x = blockIdx.x * kTxaaTW + threadIdx.x;
+    const int ya = blockIdx.y * TH + threadIdx.y, yb = ya + kTxaaTH;
+    const bool ina = x < W && ya < H, inb = x < W && yb < H;
+    const size_t oa = (size_t)ya * (size_t)W + (size_t)x, ob = (size_t)yb * (size_t)W + (size_t)x;
+    // the stored history taps, read before the tile so that the loads overlap
+    float4 ha = make_float4(0.0f, 0.0f, 0.0f, 0.0f), hb = ha;
+    if (HISTORY_IN_OUT && ina) ha = a.out[oa];
+    if (HISTORY_IN_OUT && inb) hb = a.out[ob];
     bool plain = true;
     for (int i = tid; i < SW * SH; i += kTxaaTW * kTxaaTH) {
         const int gx = x0 + i % SW, gy = y0 + i / SW;
@@ -243,20 +248,25 @@ __global__ void __launch_bounds__(kTxaaTW * kTxaaTH, 4) txaa_kernel(const __grid
     }
     // the whole tile non-negative and NaN-free: the block takes the min/max path
     plain = __syncthreads_and(plain) != 0;
-    if (!inside) return;
     auto load = [&](int i, int j) -> f4v {
         const float4 s = tile[j - y0][i - x0];
         return f4v{s.x, s.y, s.z, s.w};
     };
-    f4v prev;
-    if (HISTORY_IN_OUT) {
-        prev = f4v{h.x, h.y, h.z, h.w};
-    } else {
-        prev = txaa_history(a.vc, a.history, x, y, W, H);
+#pragma unroll 1
+    for (int r = 0; r < kTxaaRows; ++r) {
+        if (!(r == 0 ? ina : inb)) continue;
+        const int y = r == 0 ? ya : yb;
+        f4v prev;
+        if (HISTORY_IN_OUT) {
+            const float4 h = r == 0 ? ha : hb;
+            prev = f4v{h.x, h.y, h.z, h.w};
+        } else {
+            prev = txaa_history(a.vc, a.history, x, y, W, H);
+        }
+        const f4v res = plain ? txaa_resolve<true>(a.params, a.vc, prev, x, y, W, H, load)
+                              : txaa_resolve<false>(a.params, a.vc, prev, x, y, W, H, load);
+        a.out[r == 0 ? oa : ob] = make_float4(res.x, res.y, res.z, res.w);
     }
-    const f4v r = plain ? txaa_resolve<true>(a.params, a.vc, prev, x, y, W, H, load)
-                        : txaa_resolve<false>(a.params, a.vc, prev, x, y, W, H, load);
-    a.out[o] = make_float4(r.x, r.y, r.z, r.w);
 }
 
 // Reprojection fused with the TXAA resolve, after the raymarch of the frame.
@@ -424,7 +434,8 @@ cudaError_t launch_frame(const MarchArgs& a, cudaStream_t s, const LaunchEvents*
         if (e == cudaSuccess) e = cudaStreamWaitEvent(s, fj->join, 0);
         if (e != cudaSuccess) return e;
         if (timed) cudaEventRecord(ev->resolve[0], s);
-        txaa_kernel<true><<<grid, block, 0, s>>>(t);
+        const dim3 grid_r(grid.x, (unsigned)((a.height + kTxaaTH * kTxaaRows - 1) / (kTxaaTH * kTxaaRows)));
+        txaa_kernel<true><<<grid_r, block, 0, s>>>(t);
         if (timed) cudaEventRecord(ev->resolve[1], s);
         return cudaGetLastError();
     }
@@ -445,8 +456,8 @@ cudaError_t launch_selftest_division(const float* a, const float* b, float* out_
 
 cudaError_t launch_txaa(const TxaaArgs& a, cudaStream_t s, const cudaEvent_t* ev) {
     if (ev) cudaEventRecord(ev[0], s);
-    const dim3 block(kTxaaTW, kTxaaTH),
-        grid((unsigned)((a.width + kTxaaTW - 1) / kTxaaTW), (unsigned)((a.height + kTxaaTH - 1) / kTxaaTH));
+    const dim3 block(kTxaaTW, kTxaaTH), grid((unsigned)((a.width + kTxaaTW - 1) / kTxaaTW),
+                                             (unsigned)((a.height + kTxaaTH * kTxaaRows - 1) / (kTxaaTH * kTxaaRows)));
     txaa_kernel<false><<<grid, block, 0, s>>>(a);
     if (ev) cudaEventRecord(ev[1], s);
     return cudaGetLastError();

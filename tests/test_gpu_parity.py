@@ -272,6 +272,30 @@ def test_argument_errors(ctx, lib):
     torch.cuda.synchronize()
 
 
+@pytest.mark.parametrize("block", [32, 128])
+def test_march_block_sizes_give_identical_frames(ctx, block):
+    """The raymarch's CTA size (32, 128 or the default 256 threads) changes
+    neither bits nor counters."""
+    w, h = 300, 170
+    cam, tm, params, _ = scenes.config_view(23, w, h)
+    prev = to_dev(np.random.default_rng(4).random((h, w, 4), dtype=np.float32), torch)
+    outs = []
+    for b in (0, block):
+        ctx.set_tuning(march_block=b)
+        for flags in (abi.MT_RENDER_FULL, abi.MT_RENDER_CHECKERBOARD):
+            cur = torch.zeros((h, w, 4), dtype=torch.float32, device="cuda")
+            mask = torch.full((h, w), float("nan"), dtype=torch.float32, device="cuda")
+            ctx.render(cam, cam, tm, params, prev, cur, mask, flags | abi.MT_RENDER_COUNT)
+            st = ctx.stats(reset=True)
+            outs.append((cur.cpu().numpy(), mask.cpu().numpy(),
+                         (st.primary_samples, st.light_samples, st.marched_rays, st.pixels)))
+    ctx.set_tuning(march_block=0)
+    for a, b in zip(outs[:2], outs[2:]):
+        assert_bits_equal(a[0], b[0], f"block {block} rgba")
+        assert_bits_equal(a[1], b[1], f"block {block} mask")
+        assert a[2] == b[2]
+
+
 @pytest.mark.parametrize("lanes", [1, 4, 16])
 def test_march_lane_counts_give_identical_frames(ctx, lanes):
     """The step-parallel march is exact: any lane count gives the same bits and counters."""
