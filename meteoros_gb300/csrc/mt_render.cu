@@ -219,10 +219,10 @@ __global__ void __launch_bounds__(kTxaaTW * kTxaaTH) txaa_history_kernel(const _
     a.out[(size_t)y * (size_t)a.width + (size_t)x] = make_float4(h.x, h.y, h.z, h.w);
 }
 
-// The resolve: a 32x8 CTA owns a 32x16 tile, each thread two pixels 8 rows
-// apart (the halo and the barrier are shared by twice the pixels).
+// The resolve: a 32x8 CTA owns a 32x32 tile, each thread four pixels 8 rows
+// apart (the halo and the barrier are shared by four times the pixels).
 // HISTORY_IN_OUT: the history taps were stored in `out` by txaa_history_kernel.
-constexpr int kTxaaRows = 2;
+constexpr int kTxaaRows = 4;
 template <bool HISTORY_IN_OUT>
 __global__ void __launch_bounds__(kTxaaTW * kTxaaTH, 4) txaa_kernel(const __grid_constant__ TxaaArgs a) {
     constexpr int TH = kTxaaTH * kTxaaRows, SW = kTxaaTW + 3, SH = TH + 3;
@@ -231,13 +231,7 @@ __global__ void __launch_bounds__(kTxaaTW * kTxaaTH, 4) txaa_kernel(const __grid
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
     const int x0 = blockIdx.x * kTxaaTW - 1, y0 = blockIdx.y * TH - 1;
     const int x = blockIdx.x * kTxaaTW + threadIdx.x;
-    const int ya = blockIdx.y * TH + threadIdx.y, yb = ya + kTxaaTH;
-    const bool ina = x < W && ya < H, inb = x < W && yb < H;
-    const size_t oa = (size_t)ya * (size_t)W + (size_t)x, ob = (size_t)yb * (size_t)W + (size_t)x;
-    // the stored history taps, read before the tile so that the loads overlap
-    float4 ha = make_float4(0.0f, 0.0f, 0.0f, 0.0f), hb = ha;
-    if (HISTORY_IN_OUT && ina) ha = a.out[oa];
-    if (HISTORY_IN_OUT && inb) hb = a.out[ob];
+    const int ya = blockIdx.y * TH + threadIdx.y;
     bool plain = true;
     for (int i = tid; i < SW * SH; i += kTxaaTW * kTxaaTH) {
         const int gx = x0 + i % SW, gy = y0 + i / SW;
@@ -254,18 +248,19 @@ __global__ void __launch_bounds__(kTxaaTW * kTxaaTH, 4) txaa_kernel(const __grid
     };
 #pragma unroll 1
     for (int r = 0; r < kTxaaRows; ++r) {
-        if (!(r == 0 ? ina : inb)) continue;
-        const int y = r == 0 ? ya : yb;
+        const int y = ya + r * kTxaaTH;
+        if (!(x < W && y < H)) continue;
+        const size_t o = (size_t)y * (size_t)W + (size_t)x;
         f4v prev;
         if (HISTORY_IN_OUT) {
-            const float4 h = r == 0 ? ha : hb;
+            const float4 h = a.out[o];
             prev = f4v{h.x, h.y, h.z, h.w};
         } else {
             prev = txaa_history(a.vc, a.history, x, y, W, H);
         }
         const f4v res = plain ? txaa_resolve<true>(a.params, a.vc, prev, x, y, W, H, load)
                               : txaa_resolve<false>(a.params, a.vc, prev, x, y, W, H, load);
-        a.out[r == 0 ? oa : ob] = make_float4(res.x, res.y, res.z, res.w);
+        a.out[o] = make_float4(res.x, res.y, res.z, res.w);
     }
 }
 
