@@ -5,8 +5,10 @@
 // the operation order of the reference shaders, so the control flow of the
 // march (the `t += stepSize` recurrence, the `baseDensity > 0` branch and the
 // `accumDensity >= 1` exit of cloudRayMarch.comp:627-684) is reproduced exactly.
-// Only exp/pow/acos/cos (CUDA's libdevice vs the host's libm) may differ in
-// the last bits, and they feed colour only, never control flow.
+// Only the transcendentals differ from a host evaluation: acos/cos/exp/pow of
+// the sky in the last bits (CUDA's libdevice vs the host's libm), exp/pow of
+// the light energy by tens of ulp (the special-function unit's exp2/log2
+// forms).  They feed colour only, never control flow.
 //
 // Fixed meanings of what GLSL leaves to the implementation:
 //   dot = ((a.x*b.x + a.y*b.y) + a.z*b.z); normalize(v) = v / length(v);
@@ -99,7 +101,6 @@ MT_HD f3 rdiv3(f3 a, Rcp r) {
     if (rdiv_in_range(q.x) & rdiv_in_range(q.y) & rdiv_in_range(q.z)) return q;
     return rdiv3_exceptional(a.x, a.y, a.z, r);
 }
-static __device__ __noinline__ float pow_nl(float x, float y) { return powf(x, y); }
 
 MT_HD float dot3(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 MT_HD float length3(f3 a) { return sqrtf(dot3(a, a)); }

@@ -189,13 +189,17 @@ MT_HD float henyey_greenstein(float c, float e) {
 }
 
 // cloudRayMarch.comp:331-388.  cos_q = (cos_angle - 0.7) / (1.0 - 0.7), the
-// ray-constant quotient of the attenuation remap (:341-343).
+// ray-constant quotient of the attenuation remap (:341-343).  exp and pow are
+// the special-function unit's forms, exp2(x * log2 e) and exp2(y * log2 x),
+// which is how GLSL defines pow's precision: they differ from the correctly
+// rounded values by tens of ulp at most.  The light energy reaches colour
+// only, never the accumulated density, the control flow or the god-ray mask.
 MT_HD float light_energy(float h, float dl, float ds, float phase, float cos_q, float brightness) {
-    const float primary = expf(-dl);
+    const float primary = __expf(-dl);
     const float secondary = primary;  // exp(-dl) twice in the reference (:334, :340)
     float att = gmax(secondary + (cos_q * (secondary * 0.25f - secondary)), primary);
-    float depth = 0.05f + pow_nl(ds, gclamp(remap_r(h * 0.125f, 0.3f, MT_RCP(0.3f, 0.85f), 0.5f, 2.0f), 0.5f, 2.0f));
-    float vert = pow_nl(gclamp(remap_r(h * 1.5f, 0.07f, MT_RCP(0.07f, 0.34f), 0.1f, 1.0f), 0.1f, 1.0f), 0.8f);
+    float depth = 0.05f + __powf(ds, gclamp(remap_r(h * 0.125f, 0.3f, MT_RCP(0.3f, 0.85f), 0.5f, 2.0f), 0.5f, 2.0f));
+    float vert = __powf(gclamp(remap_r(h * 1.5f, 0.07f, MT_RCP(0.07f, 0.34f), 0.1f, 1.0f), 0.1f, 1.0f), 0.8f);
     float in_scatter = depth * vert;
     return att * primary * in_scatter * phase * brightness;
 }
