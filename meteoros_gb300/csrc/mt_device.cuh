@@ -93,6 +93,15 @@ MT_HD float rdiv(float a, Rcp r) {
 }
 // Three quotients by one denominator with one range check; when any falls
 // outside it, all three are redone one by one out of line.
+static __device__ __noinline__ float2 rdiv2_exceptional(float a, float b, Rcp r) {
+    return make_float2(rdiv(a, r), rdiv(b, r));
+}
+// Two quotients by one denominator, one range check.
+MT_HD float2 rdiv2(float a, float b, Rcp r) {
+    const float qa = rdiv_core(a, r), qb = rdiv_core(b, r);
+    if (rdiv_in_range(qa) & rdiv_in_range(qb)) return make_float2(qa, qb);
+    return rdiv2_exceptional(a, b, r);
+}
 static __device__ __noinline__ f3 rdiv3_exceptional(float ax, float ay, float az, Rcp r) {
     return f3{rdiv(ax, r), rdiv(ay, r), rdiv(az, r)};
 }

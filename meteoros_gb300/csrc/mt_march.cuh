@@ -52,7 +52,8 @@ template <int S> MT_HD Weather weather_at(const mt_params& p, const Frame& F, co
         w.mul = p.coverage;
         w.type = 0.0f;
     } else {
-        f4v wd = Vol<S>::template tex2<MT_WEATHER_N>(tx.weather, rdiv(pos.x - ec.x, F.r_weather), rdiv(pos.z - ec.z, F.r_weather));
+        const float2 wuv = rdiv2(pos.x - ec.x, pos.z - ec.z, F.r_weather);
+        f4v wd = Vol<S>::template tex2<MT_WEATHER_N>(tx.weather, wuv.x, wuv.y);
         w.lo = 1.0f - wd.x;
         w.mul = wd.x;
         w.type = wd.z;
@@ -146,7 +147,7 @@ MT_HD StepOut eval_step(const mt_params& p, const Frame& F, const Tex<S>& tx, co
     f3 jd = rc.dir + f3{j[0], j[1], j[2]};
     f3 pos = ld3(F.eye) + t * jd;
     f3 sp = relative_position(F, pos, ld3(F.ec));
-    sp = f3{rdiv(sp.x, F.r_period), rdiv(sp.y, F.r_period), rdiv(sp.z, F.r_period)};
+    sp = rdiv3(sp, F.r_period);
     float relH = relative_height(F, pos, ld3(F.ec), rc.lenInner, rc.dir, ld3(F.eye));
     sp = sp + ((relH * ld3(F.skew)) * p.cloud_top_offset) * 0.009f;
     sp = sp + ld3(F.wind_t);

@@ -157,13 +157,26 @@ MT_HD f3 relative_position(const Frame& F, f3 pos, f3 ec) {
     return rdiv3(pos - f3{ec.x, F.inner_alt, ec.z}, F.r_thick);
 }
 
-// cloudRayMarch.comp:475-487
+// The four quotients of height_gradient's remaps, (h - omin) / (omax - omin).
+struct HgQuot {
+    float q1, q2, q3, q4;
+};
+static __device__ __noinline__ HgQuot hg_quotients_exceptional(float h) {
+    return HgQuot{rdiv(h - 0.0f, MT_RCP(0.0f, 0.25f)), rdiv(h - 0.3f, MT_RCP(0.3f, 0.65f)),
+                  rdiv(h - 0.0f, MT_RCP(0.0f, 0.1f)), rdiv(h - 0.2f, MT_RCP(0.2f, 0.3f))};
+}
+
+// cloudRayMarch.comp:475-487.  The remaps' four quotients share one range
+// check (rdiv_core; all four redone by rdiv when any falls outside it).
 MT_HD float height_gradient(float h, float type) {
     h = gclamp(h, 0.0f, 1.0f);
-    float stratocumulus = gmax(0.0f, remap_r(h, 0.0f, MT_RCP(0.0f, 0.25f), 0.0f, 1.0f) *
-                                         remap_r(h, 0.3f, MT_RCP(0.3f, 0.65f), 1.0f, 0.0f));
-    float stratus = gmax(0.0f, remap_r(h, 0.0f, MT_RCP(0.0f, 0.1f), 0.0f, 1.0f) *
-                                   remap_r(h, 0.2f, MT_RCP(0.2f, 0.3f), 1.0f, 0.0f));
+    HgQuot q{rdiv_core(h - 0.0f, MT_RCP(0.0f, 0.25f)), rdiv_core(h - 0.3f, MT_RCP(0.3f, 0.65f)),
+             rdiv_core(h - 0.0f, MT_RCP(0.0f, 0.1f)), rdiv_core(h - 0.2f, MT_RCP(0.2f, 0.3f))};
+    if (!(rdiv_in_range(q.q1) & rdiv_in_range(q.q2) & rdiv_in_range(q.q3) & rdiv_in_range(q.q4)))
+        q = hg_quotients_exceptional(h);
+    // remap(h, omin, omax, nmin, nmax) = nmin + q * (nmax - nmin)
+    float stratocumulus = gmax(0.0f, (0.0f + (q.q1 * (1.0f - 0.0f))) * (1.0f + (q.q2 * (0.0f - 1.0f))));
+    float stratus = gmax(0.0f, (0.0f + (q.q3 * (1.0f - 0.0f))) * (1.0f + (q.q4 * (0.0f - 1.0f))));
     float a = gmix(stratus, stratocumulus, gclamp(type * 2.0f, 0.0f, 1.0f));
     float b = gmix(stratocumulus, stratus, gclamp((type - 0.5f) * 2.0f, 0.0f, 1.0f));
     return gmix(a, b, type);
