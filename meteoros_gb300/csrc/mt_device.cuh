@@ -73,9 +73,14 @@ MT_HD int f2i(float v) { return __float2int_rz(v); }
 // quotients go through the IEEE division; a zero dividend takes q0, which
 // carries the quotient's sign when y is finite.
 // ---------------------------------------------------------------------------
-// The IEEE division, out of line: one shared copy keeps the callers small in
-// the instruction cache (the march loop is instruction-fetch bound otherwise).
+// The IEEE division, out of line by default: one shared copy keeps the callers
+// small in the instruction cache (the march loop is instruction-fetch bound
+// otherwise).  Translation units of small kernels define MT_DIV_INLINE.
+#ifdef MT_DIV_INLINE
+MT_HD float div_ieee(float a, float b) { return a / b; }
+#else
 static __device__ __noinline__ float div_ieee(float a, float b) { return a / b; }
+#endif
 MT_HD Rcp make_rcp(float b) { return Rcp{b, div_ieee(1.0f, b)}; }
 MT_HD float rdiv_core(float a, Rcp r) {
     const float q0 = __fmul_rn(a, r.y);

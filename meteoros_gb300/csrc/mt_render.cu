@@ -14,7 +14,9 @@
 // kernels write disjoint pixel sets, so the outcome is defined and the two
 // launches can overlap.
 //
-// Compiled with -fmad=false: see mt_device.cuh.
+// Compiled with -fmad=false: see mt_device.cuh.  The divisions are inlined
+// (MT_DIV_INLINE): these kernels are small enough for the instruction cache.
+#define MT_DIV_INLINE 1
 #include <cuda_runtime.h>
 
 #include "mt_shared.cuh"
