@@ -5,10 +5,11 @@
 // the operation order of the reference shaders, so the control flow of the
 // march (the `t += stepSize` recurrence, the `baseDensity > 0` branch and the
 // `accumDensity >= 1` exit of cloudRayMarch.comp:627-684) is reproduced exactly.
-// Only the transcendentals differ from a host evaluation: acos/cos/exp/pow of
-// the sky in the last bits (CUDA's libdevice vs the host's libm), exp/pow of
-// the light energy by tens of ulp (the special-function unit's exp2/log2
-// forms).  They feed colour only, never control flow.
+// What differs from a host evaluation feeds colour only, never control flow:
+// acos/cos/exp/pow of the sky in the last bits (CUDA's libdevice vs the host's
+// libm), and the cone-light samples and light energy, evaluated with fused
+// multiply-adds, reciprocal products and the special-function unit's
+// exp2/log2 (a few to tens of ulp).
 //
 // Fixed meanings of what GLSL leaves to the implementation:
 //   dot = ((a.x*b.x + a.y*b.y) + a.z*b.z); normalize(v) = v / length(v);
@@ -201,6 +202,23 @@ MT_HD f4p lerp_texels(uint32_t w0, uint32_t w1, float2 t) {
 }
 
 // ---------------------------------------------------------------------------
+// Light-sample sampler: the same trilinear filter with every lerp one fused
+// multiply-add, p + t * (q - p) rounded once.  The cone-light samples reach
+// colour only (through the light energy), never the accumulated density, the
+// control flow or the god-ray mask, so they are held to the colour tolerance
+// rather than to the shader's exact operation sequence.
+// ---------------------------------------------------------------------------
+MT_HD f4p lerp_texels_fused(uint32_t w0, uint32_t w1, float2 t) {
+    const float2 bias = splat2(kByteBias);
+    const float2 P0 = biased_pair(w0, 0u), Q0 = biased_pair(w1, 0u);
+    const float2 P1 = biased_pair(w0, 2u), Q1 = biased_pair(w1, 2u);
+    return f4p{__ffma2_rn(t, sub2(Q0, P0), sub2(P0, bias)), __ffma2_rn(t, sub2(Q1, P1), sub2(P1, bias))};
+}
+MT_HD f4p lerp4p_fused(f4p p, f4p q, float2 t) {
+    return f4p{__ffma2_rn(t, sub2(q.xy, p.xy), p.xy), __ffma2_rn(t, sub2(q.zw, p.zw), p.zw)};
+}
+
+// ---------------------------------------------------------------------------
 // Samplers.  Vulkan LINEAR filter with exact FP32 weights: u = s*N - 0.5,
 // i0 = floor(u), alpha = u - i0, REPEAT wraps the integer texel coordinate
 // (N is a power of two).  Raw texel values are interpolated x, then y, then
@@ -230,6 +248,31 @@ template <int N> MT_HD f4v tex3_u8(const uint32_t* __restrict__ vol, f3 s) {
     const f4p c0 = lerp4p(c00, c10, b2);
     const f4p c1 = lerp4p(c01, c11, b2);
     return scale4p(lerp4p(c0, c1, g2), 1.0f / 255.0f);
+}
+
+// tex3_u8 with fused lerps (light samples).
+template <int N> MT_HD f4v tex3_u8_fused(const uint32_t* __restrict__ vol, f3 s) {
+    constexpr unsigned M = (unsigned)N - 1u;
+    const float fn = (float)N;
+    float u = s.x * fn - 0.5f, v = s.y * fn - 0.5f, w = s.z * fn - 0.5f;
+    float fu = floorf(u), fv = floorf(v), fw = floorf(w);
+    float a = u - fu, b = v - fv, g = w - fw;
+    unsigned iu = (unsigned)f2i(fu), iv = (unsigned)f2i(fv), iw = (unsigned)f2i(fw);
+    unsigned x0 = iu & M, x1 = (iu + 1u) & M, y0 = iv & M, y1 = (iv + 1u) & M, z0 = iw & M, z1 = (iw + 1u) & M;
+    const uint32_t* p0 = vol + (size_t)z0 * (N * N);
+    const uint32_t* p1 = vol + (size_t)z1 * (N * N);
+    uint32_t t000 = __ldg(p0 + y0 * N + x0), t100 = __ldg(p0 + y0 * N + x1);
+    uint32_t t010 = __ldg(p0 + y1 * N + x0), t110 = __ldg(p0 + y1 * N + x1);
+    uint32_t t001 = __ldg(p1 + y0 * N + x0), t101 = __ldg(p1 + y0 * N + x1);
+    uint32_t t011 = __ldg(p1 + y1 * N + x0), t111 = __ldg(p1 + y1 * N + x1);
+    const float2 a2 = splat2(a), b2 = splat2(b), g2 = splat2(g);
+    const f4p c00 = lerp_texels_fused(t000, t100, a2);
+    const f4p c10 = lerp_texels_fused(t010, t110, a2);
+    const f4p c01 = lerp_texels_fused(t001, t101, a2);
+    const f4p c11 = lerp_texels_fused(t011, t111, a2);
+    const f4p c0 = lerp4p_fused(c00, c10, b2);
+    const f4p c1 = lerp4p_fused(c01, c11, b2);
+    return scale4p(lerp4p_fused(c0, c1, g2), 1.0f / 255.0f);
 }
 
 template <int N> MT_HD f4v tex2_u8(const uint32_t* __restrict__ img, float sx, float sy) {

@@ -16,16 +16,19 @@ template <int S> struct Vol;
 template <> struct Vol<MT_STORAGE_U8> {
     using T = uint32_t;
     template <int N> static MT_HD f4v tex3(const T* v, f3 s) { return tex3_u8<N>(v, s); }
+    template <int N> static MT_HD f4v tex3_light(const T* v, f3 s) { return tex3_u8_fused<N>(v, s); }
     template <int N> static MT_HD f4v tex2(const T* v, float x, float y) { return tex2_u8<N>(v, x, y); }
 };
 template <> struct Vol<MT_STORAGE_F16> {
     using T = uint2;
     template <int N> static MT_HD f4v tex3(const T* v, f3 s) { return tex3_p16<N, __half2>(v, s); }
+    template <int N> static MT_HD f4v tex3_light(const T* v, f3 s) { return tex3_p16<N, __half2>(v, s); }
     template <int N> static MT_HD f4v tex2(const T* v, float x, float y) { return tex2_p16<N, __half2>(v, x, y); }
 };
 template <> struct Vol<MT_STORAGE_BF16> {
     using T = uint2;
     template <int N> static MT_HD f4v tex3(const T* v, f3 s) { return tex3_p16<N, __nv_bfloat162>(v, s); }
+    template <int N> static MT_HD f4v tex3_light(const T* v, f3 s) { return tex3_p16<N, __nv_bfloat162>(v, s); }
     template <int N> static MT_HD f4v tex2(const T* v, float x, float y) {
         return tex2_p16<N, __nv_bfloat162>(v, x, y);
     }
@@ -77,6 +80,23 @@ MT_HD float sample_low_frequency(const mt_params& p, const Tex<S>& tx, f3 point,
     // shared by the step's samples
     float v = gclamp(baseCloud, wt.lo, 1.0f);
     float bc = gclamp(0.0f + ((rdiv(v - wt.lo, wt.r_lo)) * (1.0f - 0.0f)), 0.0f, 1.0f);
+    return bc * wt.mul;
+}
+
+// sample_low_frequency for a cone-light sample (cloudRayMarch.comp:659-666).
+// Light samples reach colour only: fused lerps, the quotients as products with
+// the reciprocal (the remap's varying one by the fast division) and min/max
+// clamps, a few ulp from the exact sequence above.
+template <int S>
+MT_HD float sample_light(const mt_params& p, const Tex<S>& tx, f3 point, const Weather& wt) {
+    const f4v n = Vol<S>::template tex3_light<MT_BASE_N>(tx.base, point);
+    float fbm = fmaf(n.w, 0.125f, fmaf(n.z, 0.25f, n.y * 0.625f));
+    fbm = fminf(fmaxf(fbm, 0.0f), 1.0f);
+    const float lo = fbm - 0.9f;
+    float baseCloud = fminf(fmaxf(__fdividef(n.x - lo, 1.0f - lo), 0.0f), 1.0f);
+    if (p.height_gradient) baseCloud = baseCloud * wt.hgrad;
+    const float v = fminf(fmaxf(baseCloud, wt.lo), 1.0f);
+    const float bc = fminf(fmaxf((v - wt.lo) * wt.r_lo.y, 0.0f), 1.0f);
     return bc * wt.mul;
 }
 
@@ -163,14 +183,15 @@ MT_HD StepOut eval_step(const mt_params& p, const Frame& F, const Tex<S>& tx, co
         o.in_cloud = 1;
         o.hfd = erode(baseDensity * 1.4f, ero);
         float dl = 0.0f;
-        // Kept rolled: six inlined copies of the sampler overflow the
-        // instruction cache (the dominant stall when unrolled).
+        // The six cone-light samples (colour only: see sample_light).  Kept
+        // rolled: six inlined copies of the sampler overflow the instruction
+        // cache.
 #pragma unroll 1
         for (int i = 0; i < 6; ++i) {
-            f3 lightPos = pos + rc.koff[i];
-            f3 slp = relative_position(F, lightPos, ld3(F.ec));
-            float cbl = sample_low_frequency<S>(p, tx, slp, relH, wt);
-            if (cbl > 0.0f) dl = dl + erode(1.5f * cbl, ero);
+            const f3 d = (pos + rc.koff[i]) - f3{F.ec[0], F.inner_alt, F.ec[2]};
+            const f3 slp{d.x * F.r_thick.y, d.y * F.r_thick.y, d.z * F.r_thick.y};
+            const float cbl = sample_light<S>(p, tx, slp, wt);
+            if (cbl > 0.0f) dl = dl + (1.5f * cbl - ero.lo) * ero.r.y;  // erode(1.5 * cbl)
         }
         o.E = light_energy(relH, dl, baseDensity, rc.HG_light, rc.cos_q, 5.0f);
     }
