@@ -254,7 +254,7 @@ template <int N> MT_HD f4v tex3_u8(const uint32_t* __restrict__ vol, f3 s) {
 template <int N> MT_HD f4v tex3_u8_fused(const uint32_t* __restrict__ vol, f3 s) {
     constexpr unsigned M = (unsigned)N - 1u;
     const float fn = (float)N;
-    float u = s.x * fn - 0.5f, v = s.y * fn - 0.5f, w = s.z * fn - 0.5f;
+    float u = fmaf(s.x, fn, -0.5f), v = fmaf(s.y, fn, -0.5f), w = fmaf(s.z, fn, -0.5f);
     float fu = floorf(u), fv = floorf(v), fw = floorf(w);
     float a = u - fu, b = v - fv, g = w - fw;
     unsigned iu = (unsigned)f2i(fu), iv = (unsigned)f2i(fv), iw = (unsigned)f2i(fw);

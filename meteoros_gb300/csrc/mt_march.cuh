@@ -115,7 +115,7 @@ template <int S> MT_HD float erosion_modifier(const Tex<S>& tx, f3 point, float 
 // per-frame ones are in Frame).
 struct RayConsts {
     f3 dir, startPos;
-    f3 koff[6];  // cone-light offsets: (stepSize * kernel[i]) * i
+    f3 koff[6];  // cone-light offsets ((stepSize * kernel[i]) * i) / thickness
     float stepSize, cos_angle, cos_q, HG_light, lenInner;
 };
 
@@ -145,7 +145,8 @@ MT_HD void ray_consts(const mt_params& p, const Frame& F, f3 dir, f3 startPos, f
                           mat3mul(xC, lightDir, zC, f3{0.0f, 3.0f, 0.0f})};
     // the step-independent part of the light sample position
     // pos + ((stepSize * kernel[i]) * i) (cloudRayMarch.comp:656)
-    for (int i = 0; i < 6; ++i) rc.koff[i] = (stepSize * kernel[i]) * (float)i;
+    // in units of the layer thickness, as the light samples' positions are used
+    for (int i = 0; i < 6; ++i) rc.koff[i] = ((stepSize * kernel[i]) * (float)i) * F.r_thick.y;
     rc.lenInner = length3(startPos - ld3(F.eye));
 }
 
@@ -186,12 +187,17 @@ MT_HD StepOut eval_step(const mt_params& p, const Frame& F, const Tex<S>& tx, co
         // The six cone-light samples (colour only: see sample_light).  Kept
         // rolled: six inlined copies of the sampler overflow the instruction
         // cache.
+        // relative_position(pos + offset) = (pos - base) / thickness + offset / thickness.
+        // Explicit roundings and fmas: the same bits in every kernel that
+        // inlines this, whatever the compiler's contraction setting.
+        const f3 pb = pos - f3{F.ec[0], F.inner_alt, F.ec[2]};
+        const f3 prel{__fmul_rn(pb.x, F.r_thick.y), __fmul_rn(pb.y, F.r_thick.y), __fmul_rn(pb.z, F.r_thick.y)};
 #pragma unroll 1
         for (int i = 0; i < 6; ++i) {
-            const f3 d = (pos + rc.koff[i]) - f3{F.ec[0], F.inner_alt, F.ec[2]};
-            const f3 slp{d.x * F.r_thick.y, d.y * F.r_thick.y, d.z * F.r_thick.y};
+            const f3 k = rc.koff[i];
+            const f3 slp{__fadd_rn(prel.x, k.x), __fadd_rn(prel.y, k.y), __fadd_rn(prel.z, k.z)};
             const float cbl = sample_light<S>(p, tx, slp, wt);
-            if (cbl > 0.0f) dl = dl + (1.5f * cbl - ero.lo) * ero.r.y;  // erode(1.5 * cbl)
+            if (cbl > 0.0f) dl = fmaf(fmaf(1.5f, cbl, -ero.lo), ero.r.y, dl);  // erode(1.5 * cbl)
         }
         o.E = light_energy(relH, dl, baseDensity, rc.HG_light, rc.cos_q, 5.0f);
     }
