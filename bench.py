@@ -558,6 +558,15 @@ def run_gb300(args) -> int:
                           "flops_per_launch": int(march_flops),
                           "peak_source": "nominal: SMs x 128 FP32 lanes x max SM clock, one non-fused op per lane "
                                          "per clock (the kernels are built without contraction)"},
+        # filtered texel fetches of the raymarch from the exact counters: per primary
+        # sample one weather (bilinear) and at most one base (trilinear) fetch;
+        # per in-cloud sample (light / 6) one curl and one detail fetch; per light
+        # sample one base fetch.  An upper bound: empty steps skip the base fetch.
+        "filtered_fetches": {
+            "trilinear_per_frame_max": int(samples_per_frame + light_per_frame * (1 + 1 / 6)),
+            "bilinear_per_frame": int(samples_per_frame + light_per_frame / 6),
+            "gtexels_per_s_max": round((8 * (samples_per_frame + light_per_frame * (1 + 1 / 6)) +
+                                        4 * (samples_per_frame + light_per_frame / 6)) / (march_ms * 1e-3) / 1e9, 1)},
         "frame_hbm": {"algorithmic_bytes": frame_bytes,
                       "achieved_gbs": round(frame_bytes / (ms * 1e-3) / 1e9, 2)},
         "clocks": clk,
