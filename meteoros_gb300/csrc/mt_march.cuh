@@ -37,7 +37,8 @@ template <> struct Vol<MT_STORAGE_BF16> {
 struct Weather {
     float lo, mul, type;
     float hgrad;  // height gradient at the primary sample, shared by its light samples
-    Rcp r_lo;     // 1 - lo, the coverage remap's width, shared by the step's samples
+    Rcp r_lo;     // {1 - lo, ~1/(1 - lo)}: the coverage remap's width (b, exact division)
+                  // and an approximate reciprocal for the light samples (y)
 };
 
 template <int S> struct Tex {
@@ -61,7 +62,7 @@ template <int S> MT_HD Weather weather_at(const mt_params& p, const Frame& F, co
         w.mul = wd.x;
         w.type = wd.z;
     }
-    w.r_lo = make_rcp(1.0f - w.lo);
+    w.r_lo = Rcp{1.0f - w.lo, __fdividef(1.0f, 1.0f - w.lo)};
     return w;
 }
 
@@ -76,10 +77,10 @@ MT_HD float sample_low_frequency(const mt_params& p, const Tex<S>& tx, f3 point,
     // the primary sample's height and weather, so it is evaluated once per step
     // (Weather::hgrad).
     if (p.height_gradient) baseCloud = baseCloud * wt.hgrad;
-    // remapClampedBeforeAndAfter(baseCloud, lo, 1, 0, 1) with its width 1 - lo
-    // shared by the step's samples
+    // remapClampedBeforeAndAfter(baseCloud, lo, 1, 0, 1), its width 1 - lo
+    // computed once per step
     float v = gclamp(baseCloud, wt.lo, 1.0f);
-    float bc = gclamp(0.0f + ((rdiv(v - wt.lo, wt.r_lo)) * (1.0f - 0.0f)), 0.0f, 1.0f);
+    float bc = gclamp(0.0f + (((v - wt.lo) / wt.r_lo.b) * (1.0f - 0.0f)), 0.0f, 1.0f);
     return bc * wt.mul;
 }
 

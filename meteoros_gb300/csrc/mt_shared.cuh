@@ -184,15 +184,16 @@ MT_HD float height_gradient(float h, float type) {
 
 struct Erosion {
     float lo;  // high_freq_modifier * 0.005
-    Rcp r;     // 1 - lo, shared by the step's seven erosions
+    Rcp r;     // {1 - lo, ~1/(1 - lo)}: the width (b, exact division) and an
+               // approximate reciprocal for the light samples (y)
 };
 MT_HD Erosion make_erosion(float modifier) {
     Erosion e;
     e.lo = modifier * 0.005f;
-    e.r = make_rcp(1.0f - e.lo);
+    e.r = Rcp{1.0f - e.lo, __fdividef(1.0f, 1.0f - e.lo)};
     return e;
 }
-MT_HD float erode(float baseCloud, const Erosion& e) { return remap_r(baseCloud, e.lo, e.r, 0.0f, 1.0f); }
+MT_HD float erode(float baseCloud, const Erosion& e) { return 0.0f + (((baseCloud - e.lo) / e.r.b) * (1.0f - 0.0f)); }
 
 // cloudRayMarch.comp:295-306
 MT_HD float henyey_greenstein(float c, float e) {
