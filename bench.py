@@ -458,26 +458,50 @@ def run_gb300(args) -> int:
     rays_per_frame = st.marched_rays / args.steps
 
     # ---- end to end through the public API: host output buffers ----
-    out_host = torch.empty((HEIGHT, WIDTH, 4), dtype=torch.float32, pin_memory=True)
-    mask_host = torch.empty((HEIGHT, WIDTH), dtype=torch.float32, pin_memory=True)
+    # (1) pipelined, as a renderer runs: K frames issued back to back through
+    # Session.frame; each frame's resolved image and god-ray mask are copied to
+    # pinned host memory on a copy stream while the next frame renders (the
+    # session double-buffers both); ms/frame = wall time / K, host clock, until
+    # the last copy has landed.  No L2 flush: every frame reads and writes
+    # ~150 MB (previous frame, history, outputs), more than the 129 MB L2.
+    out_host = [torch.empty((HEIGHT, WIDTH, 4), dtype=torch.float32, pin_memory=True) for _ in range(2)]
+    mask_host = [torch.empty((HEIGHT, WIDTH), dtype=torch.float32, pin_memory=True) for _ in range(2)]
+    copy_stream = torch.cuda.Stream(dev)
+    copied = [torch.cuda.Event() for _ in range(2)]
     e2e_sess = Session(ctx, WIDTH, HEIGHT, txaa=True)
     for i in range(args.warmup):
         e2e_sess.frame(frames[i], stream=stream)
         e2e_sess.output.cpu()
     torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        p = e2e_sess.parity  # the buffers this frame writes
+        if k >= 2:
+            stream.wait_event(copied[p])  # frame k-2's copy out of them has landed
+        e2e_sess.frame(frames[args.warmup + k], stream=stream)
+        rendered = torch.cuda.Event()
+        rendered.record(stream)
+        copy_stream.wait_event(rendered)
+        with torch.cuda.stream(copy_stream):
+            out_host[p].copy_(e2e_sess.output, non_blocking=True)
+            mask_host[p].copy_(e2e_sess.mask, non_blocking=True)
+            copied[p].record(copy_stream)
+    torch.cuda.synchronize()
+    e2e_ms = 1000.0 * (time.perf_counter() - t0) / args.steps
+    # (2) one frame at a time: L2 flushed, then the frame and its copies, waited for
     e2e_times = []
     for k in range(args.steps):
         flush.fill_(float(k))
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         e2e_sess.frame(frames[args.warmup + k], stream=stream)
-        out_host.copy_(e2e_sess.output, non_blocking=True)
-        mask_host.copy_(e2e_sess.mask, non_blocking=True)
+        out_host[0].copy_(e2e_sess.output, non_blocking=True)
+        mask_host[0].copy_(e2e_sess.mask, non_blocking=True)
         stream.synchronize()
         e2e_times.append(time.perf_counter() - t0)
-    e2e_ms = 1000.0 * sum(e2e_times) / len(e2e_times)
+    e2e_serial_ms = 1000.0 * sum(e2e_times) / len(e2e_times)
     ubo_bytes = 2 * 160 + 80 + 280  # camera, camera_old, time, params per frame (kernel parameters)
-    d2h = out_host.numel() * 4 + mask_host.numel() * 4
+    d2h = out_host[0].numel() * 4 + mask_host[0].numel() * 4
 
     if world > 1:
         dist.barrier()
@@ -571,7 +595,11 @@ def run_gb300(args) -> int:
                       "achieved_gbs": round(frame_bytes / (ms * 1e-3) / 1e9, 2)},
         "clocks": clk,
         "e2e": {"value": round(e2e_ms, 4), "unit": UNIT, "h2d_bytes_per_step": ubo_bytes,
-                "d2h_bytes_per_step": d2h},
+                "d2h_bytes_per_step": d2h,
+                "mode": "pipelined: frames issued back to back, each frame's image and mask copied to pinned "
+                        "host memory on a copy stream during the next frame; wall time / frames",
+                "serial_value": round(e2e_serial_ms, 4),
+                "serial_mode": "one frame at a time, L2 flushed, frame + copies waited for"},
         # per frame: raymarch, reprojection, TXAA history taps, TXAA resolve
         "gpu_launches": 4 * args.steps,
         "wall_s_timed": round(wall, 3),

@@ -201,7 +201,9 @@ class FrameInputs:
 
 class Session:
     """One view's temporal state on the device: raw frames for reprojection,
-    resolved frames for TXAA history, and the god-ray mask."""
+    resolved frames for TXAA history, and the god-ray masks.  Every buffer is
+    double-buffered, so a frame's results can be read back while the next
+    frame renders."""
 
     def __init__(self, ctx: Context, width: int, height: int, txaa: bool = True):
         import torch
@@ -210,9 +212,14 @@ class Session:
         dev = torch.device("cuda", ctx.device)
         self.raw = [torch.zeros((height, width, 4), dtype=torch.float32, device=dev) for _ in range(2)]
         self.resolved = [torch.zeros((height, width, 4), dtype=torch.float32, device=dev) for _ in range(2)]
-        self.mask = torch.zeros((height, width), dtype=torch.float32, device=dev)
+        self.masks = [torch.zeros((height, width), dtype=torch.float32, device=dev) for _ in range(2)]
         self.parity = 0
         self.frames = 0
+
+    @property
+    def mask(self):
+        """The last frame's god-ray mask."""
+        return self.masks[self.parity ^ 1]
 
     @property
     def output(self):
@@ -228,9 +235,9 @@ class Session:
         fl = flags if self.frames > 0 else (flags | abi.MT_RENDER_FULL)
         if self.use_txaa and self.frames > 0:
             self.ctx.render_frame(f.camera, f.camera_old, f.time, f.params, prev, cur, self.resolved[self.parity ^ 1],
-                                  self.resolved[self.parity], self.mask, fl, stream)
+                                  self.resolved[self.parity], self.masks[self.parity], fl, stream)
         else:
-            self.ctx.render(f.camera, f.camera_old, f.time, f.params, prev, cur, self.mask, fl, stream)
+            self.ctx.render(f.camera, f.camera_old, f.time, f.params, prev, cur, self.masks[self.parity], fl, stream)
             if self.use_txaa:  # first frame: the frame is its own history
                 self.ctx.txaa(f.camera, f.camera_old, f.time, f.params, cur, cur, self.resolved[self.parity], stream)
         self.parity ^= 1
