@@ -35,7 +35,6 @@ struct f4v {
     float x, y, z, w;
 };
 
-MT_HD f3 mk3(float x, float y, float z) { return f3{x, y, z}; }
 MT_HD f3 operator+(f3 a, f3 b) { return f3{a.x + b.x, a.y + b.y, a.z + b.z}; }
 MT_HD f3 operator-(f3 a, f3 b) { return f3{a.x - b.x, a.y - b.y, a.z - b.z}; }
 MT_HD f3 operator-(f3 a) { return f3{-a.x, -a.y, -a.z}; }
@@ -126,7 +125,6 @@ MT_HD f3 cross3(f3 a, f3 b) { return f3{a.y * b.z - b.y * a.z, a.z * b.x - b.z *
 MT_HD f3 mix3(f3 x, f3 y, float a) { return f3{gmix(x.x, y.x, a), gmix(x.y, y.y, a), gmix(x.z, y.z, a)}; }
 MT_HD f4v min4(f4v a, f4v b) { return f4v{gmin(a.x, b.x), gmin(a.y, b.y), gmin(a.z, b.z), gmin(a.w, b.w)}; }
 MT_HD f4v max4(f4v a, f4v b) { return f4v{gmax(a.x, b.x), gmax(a.y, b.y), gmax(a.z, b.z), gmax(a.w, b.w)}; }
-MT_HD f4v mix4(f4v x, f4v y, float a) { return f4v{gmix(x.x, y.x, a), gmix(x.y, y.y, a), gmix(x.z, y.z, a), gmix(x.w, y.w, a)}; }
 MT_HD f3 ld3(const float* p) { return f3{p[0], p[1], p[2]}; }
 
 // GLSL mat3(c0,c1,c2) * v
@@ -136,9 +134,6 @@ MT_HD f3 mat3mul(f3 c0, f3 c1, f3 c2, f3 v) {
 }
 
 MT_HD float lerp1(float p, float q, float t) { return p + t * (q - p); }
-MT_HD f4v lerp4(f4v p, f4v q, float t) {
-    return f4v{lerp1(p.x, q.x, t), lerp1(p.y, q.y, t), lerp1(p.z, q.z, t), lerp1(p.w, q.w, t)};
-}
 
 // ---------------------------------------------------------------------------
 // Packed FP32 pairs: the f32x2 add and multiply-add instructions of sm_100 and

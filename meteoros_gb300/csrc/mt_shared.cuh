@@ -135,11 +135,6 @@ MT_HD float remap_clamped(float v, float omin, float omax, float nmin, float nma
     float t = nmin + (((v - omin) / (omax - omin)) * (nmax - nmin));
     return gclamp(t, nmin, nmax);
 }
-MT_HD float remap_clamped_ba(float v, float omin, float omax, float nmin, float nmax) {
-    v = gclamp(v, omin, omax);
-    float t = nmin + (((v - omin) / (omax - omin)) * (nmax - nmin));
-    return gclamp(t, nmin, nmax);
-}
 
 // cloudRayMarch.comp:171-186
 // lenInner = length(startPos - eye) is the same for every step of a ray; the
