@@ -565,6 +565,8 @@ def run_gb300(args) -> int:
         "config": {"workload": "config1: 1920x1080 reprojected frame, 1/16 pixels raymarched (128 steps, 6 cone "
                                "light steps, Bayer 4x4 order) + 10-tap reprojection + TXAA (history 0.9)",
                    "width": WIDTH, "height": HEIGHT, "l2": "flushed between frames (256 MiB write)",
+                   "e2e_l2": "pipelined e2e not flushed: each frame reads and writes ~150 MB, more than the "
+                             "129 MB L2; the serial e2e figure is flushed",
                    "parallelism": f"replicas x{world}"},
         "gsamples_per_s": round(gsps, 4),
         "primary_samples_per_frame": int(samples_per_frame),
