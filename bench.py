@@ -208,6 +208,47 @@ def _timed_reps(torch, flush, fn, reps):
     return statistics.mean(out)
 
 
+def bench_config0(ctx, torch, flush, cpu: bool, reps: int = 5) -> dict:
+    """Config 0: 960x540 frames marching every pixel (all 16 slots), 128
+    steps, seeded views (yaw U[0,360), pitch U[5,30] deg, sun on the upper
+    hemisphere); the GPU per frame, and the CPU restatement of the reference's
+    shaders on all host cores on the first two views."""
+    import numpy as np
+
+    from meteoros_gb300 import abi, scenes
+
+    W0, H0 = 960, 540
+    views = [scenes.config_view(SEED + i, W0, H0) for i in range(reps)]
+    cur = torch.empty((H0, W0, 4), dtype=torch.float32, device="cuda")
+    mask = torch.empty((H0, W0), dtype=torch.float32, device="cuda")
+    ctx.stats(reset=True)
+    for cam, tm, params, _ in views:
+        ctx.render(cam, cam, tm, params, None, cur, mask, abi.MT_RENDER_FULL | abi.MT_RENDER_COUNT)
+    samples = ctx.stats(reset=True).primary_samples / reps
+    k = iter(range(10 ** 9))
+
+    def one():
+        cam, tm, params, _ = views[next(k) % reps]
+        ctx.render(cam, cam, tm, params, None, cur, mask, abi.MT_RENDER_FULL)
+    ms = _timed_reps(torch, flush, one, 2 * reps)
+    out = {"width": W0, "height": H0, "ms": round(ms, 4), "gsamples_per_s": round(samples / (ms * 1e-3) / 1e9, 3),
+           "primary_samples_per_frame": int(samples)}
+    if cpu:
+        from oracle import pyoracle
+
+        vols = pyoracle.generate_volumes(SEED)
+        vol = pyoracle.Volumes(vols["base"], vols["detail"], vols["curl"], vols["weather"])
+        times = []
+        for cam, tm, params, _ in views[:2]:
+            t0 = time.perf_counter()
+            pyoracle.render(vol, cam, cam, tm, params, None, W0, H0, abi.MT_RENDER_FULL)
+            times.append(time.perf_counter() - t0)
+        out["cpu_ms"] = round(1000.0 * statistics.mean(times), 3)
+        out["cpu_cores"] = os.cpu_count() or 1
+        out["cpu_sample"] = "2 views, the CPU restatement of the reference's shaders, OpenMP over rows"
+    return out
+
+
 def bench_batched(ctx, torch, flush, reps: int = 3) -> dict:
     """Config 3: 64 views of uneven resolution, full raymarch, step budgets
     U{64..128}, per-view weather maps (seed + view id), one persistent
@@ -546,7 +587,8 @@ def run_gb300(args) -> int:
     if world == 1 and not args.no_forms:
         forms = {}
         n = args.serve_requests
-        for name, fn in (("batched_config3", lambda: bench_batched(ctx, torch, flush)),
+        for name, fn in (("full_frame_config0", lambda: bench_config0(ctx, torch, flush, not args.no_cpu_baseline)),
+                         ("batched_config3", lambda: bench_batched(ctx, torch, flush)),
                          ("precision_config2", lambda: bench_precision(ctx, torch, flush)),
                          ("serve_config4", lambda: bench_serving(ctx, torch, n, False)),
                          ("serve_config4_graph", lambda: bench_serving(ctx, torch, n, False, use_graph=True)),
