@@ -22,7 +22,9 @@ and the reported time is the max over ranks.
 CPU restatement of its shaders (oracle/), which the tests pin bit-exact
 against the reference's own shader source compiled as C++.  The reference's
 shaders hard-code other constants than config 1's, so the source itself
-cannot run this workload.
+cannot run this workload.  That arm builds its uniform blocks with the
+oracle's restatement of the reference's producers (pinned bit for bit to the
+library's) and never loads the CUDA library.
 """
 from __future__ import annotations
 
@@ -74,6 +76,16 @@ def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return rank, world, local
+
+
+def workload_config(world: int) -> dict:
+    """The `config` object of the JSON line; both arms print this same dict."""
+    return {"workload": "config1: 1920x1080 reprojected frame, 1/16 pixels raymarched (128 steps, 6 cone "
+                        "light steps, Bayer 4x4 order) + 10-tap reprojection + TXAA (history 0.9)",
+            "width": WIDTH, "height": HEIGHT, "l2": "flushed between frames (256 MiB write)",
+            "e2e_l2": "pipelined e2e not flushed: each frame reads and writes ~150 MB, more than the "
+                      "129 MB L2; the serial e2e figure is flushed",
+            "parallelism": f"replicas x{world}"}
 
 
 # ---------------------------------------------------------------------------
@@ -136,15 +148,13 @@ def cpu_frames(n_warmup: int, n_frames_max: int, seconds: float):
     reference's shader source on the reference constants; config 1's
     weather-driven parameters exist only in the restatement).
     Returns (ms_per_frame, frames, cores, primary_samples)."""
-    import numpy as np
-
-    from meteoros_gb300 import abi, scenes
+    from meteoros_gb300 import abi, scenes  # abi: struct types and constants only
     from oracle import pyoracle
 
     cores = os.cpu_count() or 1
     vols = pyoracle.generate_volumes(SEED)
     vol = pyoracle.Volumes(vols["base"], vols["detail"], vols["curl"], vols["weather"])
-    seq = scenes.config_sequence(SEED, WIDTH, HEIGHT, frames=1 + n_warmup + n_frames_max)
+    seq = scenes.config_sequence(SEED, WIDTH, HEIGHT, frames=1 + n_warmup + n_frames_max, uniforms=pyoracle)
     # frame 0 of the sequence marches every pixel (no previous frame)
     cam, old, tm, params = seq[0]
     prev, _, _ = pyoracle.render(vol, cam, old, tm, params, None, WIDTH, HEIGHT, abi.MT_RENDER_FULL)
@@ -178,9 +188,9 @@ def run_reference(args) -> int:
     line = {
         "impl": "reference", "metric": METRIC, "value": round(ms, 3), "unit": UNIT, "n_gpus": args.gpus,
         "steps": frames, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": False,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator volumes)",
-        "config": {"workload": "config1: 1920x1080 reprojected frame (1/16 marched, 128 steps, 6 light "
-                               "steps) + TXAA, CPU", "steps_per_frame": "checkerboard + reprojection + TXAA"},
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded generator volumes, seeded cameras)",
+        "config": workload_config(world),
         "cpu_baseline": {"value": round(ms, 3), "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"{frames} full 1080p frames of the config-1 sequence"},
         "e2e": {"value": round(ms, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -604,12 +614,7 @@ def run_gb300(args) -> int:
         "metric": METRIC, "value": round(ms, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator volumes, seeded cameras)",
-        "config": {"workload": "config1: 1920x1080 reprojected frame, 1/16 pixels raymarched (128 steps, 6 cone "
-                               "light steps, Bayer 4x4 order) + 10-tap reprojection + TXAA (history 0.9)",
-                   "width": WIDTH, "height": HEIGHT, "l2": "flushed between frames (256 MiB write)",
-                   "e2e_l2": "pipelined e2e not flushed: each frame reads and writes ~150 MB, more than the "
-                             "129 MB L2; the serial e2e figure is flushed",
-                   "parallelism": f"replicas x{world}"},
+        "config": workload_config(world),
         "gsamples_per_s": round(gsps, 4),
         "primary_samples_per_frame": int(samples_per_frame),
         "light_samples_per_frame": int(light_per_frame),

@@ -37,7 +37,7 @@ FAST = ["--use_fast_math"]
 
 # translation unit -> extra flags
 UNITS = {
-    "mt_host.cpp": ["-x", "cu"],
+    "mt_host.cpp": ["-x", "cu", "-Xcompiler", "-ffp-contract=off"],
     "mt_capi.cu": [],
     "mt_server.cpp": ["-x", "cu"],
     "mt_render.cu": EXACT,

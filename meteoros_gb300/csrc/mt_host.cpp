@@ -23,9 +23,10 @@ struct v3 {
 inline v3 sub(v3 a, v3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
 inline float dot(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 inline v3 cross(v3 a, v3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+// glm::normalize: v * inversesqrt(dot(v, v)) with inversesqrt(x) = 1 / sqrt(x)
 inline v3 normalize(v3 a) {
-    float l = std::sqrt(dot(a, a));
-    return {a.x / l, a.y / l, a.z / l};
+    const float inv = 1.0f / std::sqrt(dot(a, a));
+    return {a.x * inv, a.y * inv, a.z * inv};
 }
 
 // 4x4 Bayer matrix: the slot of frame i is the position holding i.

@@ -10,6 +10,12 @@ uniform blocks deterministically from a seed:
                     pitch in [5,30] deg, sun uniform on the upper hemisphere,
                     wind 10 m/s at heading 45 deg (mt_params_config)
   config_sequence   16 frames yawing 0.5 deg/frame with t += 0.16 s/frame
+
+`uniforms` names the module that produces the uniform blocks and presets:
+meteoros_gb300.abi (the library's mt_camera_look_at, mt_time_init,
+mt_params_config, mt_params_reference) by default; any module with functions
+of the same names and signatures can stand in (a host-only caller that must
+not load the CUDA library passes its own).
 """
 from __future__ import annotations
 
@@ -25,10 +31,11 @@ def _forward(yaw_deg: float, pitch_deg: float):
     return (math.cos(p) * math.sin(y), math.sin(p), -math.cos(p) * math.cos(y))
 
 
-def look(eye, yaw_deg: float, pitch_deg: float, fovy_deg: float, width: int, height: int) -> abi.CameraUBO:
+def look(eye, yaw_deg: float, pitch_deg: float, fovy_deg: float, width: int, height: int,
+         uniforms=abi) -> abi.CameraUBO:
     f = _forward(yaw_deg, pitch_deg)
     ref = tuple(e + d for e, d in zip(eye, f))
-    return abi.camera_look_at(eye, ref, fovy_deg, width / height, 0.1, 1000.0)
+    return uniforms.camera_look_at(eye, ref, fovy_deg, width / height, 0.1, 1000.0)
 
 
 def sun_direction(rng: np.random.Generator):
@@ -46,36 +53,37 @@ def set_sun(params: abi.Params, direction, distance: float = 1.0e9) -> abi.Param
     return params
 
 
-def reference_frame(width: int, height: int, pitch_deg: float = 0.0, frame: int = 0, t: float = 0.0):
+def reference_frame(width: int, height: int, pitch_deg: float = 0.0, frame: int = 0, t: float = 0.0,
+                    uniforms=abi):
     """The reference's camera and constants (REF preset)."""
-    cam = look((0.0, 0.0, 2.0), 0.0, pitch_deg, 45.0, width, height)
-    tm = abi.time_init()
+    cam = look((0.0, 0.0, 2.0), 0.0, pitch_deg, 45.0, width, height, uniforms)
+    tm = uniforms.time_init()
     tm.frame_count_mod16 = frame % 16
     tm.time[1] = t
-    return cam, tm, abi.params_reference()
+    return cam, tm, uniforms.params_reference()
 
 
-def config_view(seed: int, width: int, height: int, steps: int | None = None):
+def config_view(seed: int, width: int, height: int, steps: int | None = None, uniforms=abi):
     """Camera, time and params of one benchmark view (configs 0, 2, 3)."""
     rng = np.random.default_rng(seed)
     yaw = float(rng.uniform(0.0, 360.0))
     pitch = float(rng.uniform(5.0, 30.0))
-    cam = look((0.0, 100.0, 0.0), yaw, pitch, 60.0, width, height)
-    params = set_sun(abi.params_config(), sun_direction(rng))
+    cam = look((0.0, 100.0, 0.0), yaw, pitch, 60.0, width, height, uniforms)
+    params = set_sun(uniforms.params_config(), sun_direction(rng))
     if steps is not None:
         params.steps_min = params.steps_max = int(steps)
-    tm = abi.time_init()
+    tm = uniforms.time_init()
     return cam, tm, params, (yaw, pitch)
 
 
 def config_sequence(seed: int, width: int, height: int, frames: int = 16, yaw_step: float = 0.5,
-                    dt: float = 0.16):
+                    dt: float = 0.16, uniforms=abi):
     """Per-frame (camera, camera_old, time, params) of the reprojected sequence (config 1)."""
-    cam0, tm, params, (yaw, pitch) = config_view(seed, width, height)
+    cam0, tm, params, (yaw, pitch) = config_view(seed, width, height, uniforms=uniforms)
     out = []
     old = cam0
     for i in range(frames):
-        cam = look((0.0, 100.0, 0.0), yaw + yaw_step * i, pitch, 60.0, width, height)
+        cam = look((0.0, 100.0, 0.0), yaw + yaw_step * i, pitch, 60.0, width, height, uniforms)
         t = abi.TimeUBO()
         C_copy(t, tm)
         t.frame_count_mod16 = i % 16

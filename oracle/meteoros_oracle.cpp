@@ -849,6 +849,18 @@ __attribute__((visibility("default"))) int orc_march_pixels_f64(const orc_volume
 }
 
 // Single-function probes for the unit tests (float instantiation).
+__attribute__((visibility("default"))) float orc_height_gradient(float h, float type) {
+    return orc::height_gradient<float>(h, type);
+}
+__attribute__((visibility("default"))) float orc_remap(float v, float a, float b, float c, float d) {
+    return orc::remap<float>(v, a, b, c, d);
+}
+__attribute__((visibility("default"))) float orc_remap_clamped(float v, float a, float b, float c, float d) {
+    return orc::remap_clamped<float>(v, a, b, c, d);
+}
+__attribute__((visibility("default"))) float orc_remap_clamped_ba(float v, float a, float b, float c, float d) {
+    return orc::remap_clamped_ba<float>(v, a, b, c, d);
+}
 __attribute__((visibility("default"))) float orc_hg(float c, float e) { return orc::henyey_greenstein<float>(c, e); }
 __attribute__((visibility("default"))) float orc_light_energy(float h, float dl, float ds, float phase, float cosA,
                                                               float step, float bright) {

@@ -19,7 +19,7 @@ ORACLE_DIR = Path(__file__).resolve().parent
 BUILD_DIR = ORACLE_DIR / "_build"
 LIB = BUILD_DIR / "liboracle.so"
 SOURCES = [ORACLE_DIR / "meteoros_oracle.cpp", ORACLE_DIR / "noise_oracle.cpp", ORACLE_DIR / "post_oracle.cpp",
-           ORACLE_DIR / "asset_oracle.cpp"]
+           ORACLE_DIR / "asset_oracle.cpp", ORACLE_DIR / "uniform_oracle.cpp"]
 HEADERS = [ORACLE_DIR / "oracle_math.hpp", ORACLE_DIR.parent / "include" / "meteoros.h"]
 
 CXXFLAGS = ["-O3", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-std=c++17"]
@@ -93,8 +93,56 @@ def lib() -> C.CDLL:
         L.orc_ray_sphere.argtypes = [P, P, P, C.c_float, P]
         L.orc_tex3.restype = None
         L.orc_tex3.argtypes = [P, C.c_int, C.c_int, P, P]
+        for name, n in (("orc_height_gradient", 2), ("orc_remap", 5), ("orc_remap_clamped", 5),
+                        ("orc_remap_clamped_ba", 5)):
+            getattr(L, name).restype = C.c_float
+            getattr(L, name).argtypes = [C.c_float] * n
+        L.orc_halton.restype = C.c_float
+        L.orc_halton.argtypes = [C.c_int, C.c_int]
+        L.orc_time_init.restype = None
+        L.orc_time_init.argtypes = [tm]
+        L.orc_camera_look_at.restype = None
+        L.orc_camera_look_at.argtypes = [cam, C.POINTER(C.c_float), C.POINTER(C.c_float)] + [C.c_float] * 4
+        L.orc_params_reference.restype = None
+        L.orc_params_reference.argtypes = [par]
+        L.orc_params_config.restype = None
+        L.orc_params_config.argtypes = [par]
         _lib = L
     return _lib
+
+
+# ---------------------------------------------------------------------------
+# Uniform producers and presets, restated (uniform_oracle.cpp).  Same names and
+# signatures as meteoros_gb300.abi's, so scene builders can take either.
+# ---------------------------------------------------------------------------
+def halton(index: int, base: int) -> float:
+    return lib().orc_halton(index, base)
+
+
+def time_init() -> abi.TimeUBO:
+    t = abi.TimeUBO()
+    lib().orc_time_init(C.byref(t))
+    return t
+
+
+def camera_look_at(eye, ref, fovy_deg: float, aspect: float, near: float = 0.1,
+                   far: float = 1000.0) -> abi.CameraUBO:
+    cam = abi.CameraUBO()
+    lib().orc_camera_look_at(C.byref(cam), (C.c_float * 3)(*eye), (C.c_float * 3)(*ref), fovy_deg, aspect, near,
+                             far)
+    return cam
+
+
+def params_reference() -> abi.Params:
+    p = abi.Params()
+    lib().orc_params_reference(C.byref(p))
+    return p
+
+
+def params_config() -> abi.Params:
+    p = abi.Params()
+    lib().orc_params_config(C.byref(p))
+    return p
 
 
 def _ptr(a: np.ndarray | None):

@@ -44,6 +44,10 @@ def lib() -> C.CDLL:
         L.ref_godrays.argtypes = [cam, P, P, P, P, C.c_int, C.c_int]
         L.ref_tonemap.restype = C.c_int
         L.ref_tonemap.argtypes = [tm, P, P, C.c_int, C.c_int]
+        for name, n in (("ref_height_gradient", 2), ("ref_remap", 5), ("ref_remap_clamped", 5),
+                        ("ref_remap_clamped_ba", 5)):
+            getattr(L, name).restype = C.c_float
+            getattr(L, name).argtypes = [C.c_float] * n
         L.ref_wang_hash_noise.restype = C.c_float
         L.ref_wang_hash_noise.argtypes = [C.c_uint, C.c_uint, C.c_uint]
         _lib = L

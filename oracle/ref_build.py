@@ -39,7 +39,9 @@ ORACLE = Path(__file__).resolve().parent
 OUT = ORACLE / "_ref"
 GEN = OUT / "gen"
 LIB = OUT / "libmeteoros_ref.so"
-DEFAULT_REF = Path(os.environ.get("METEOROS_REFERENCE", "/root/reference"))
+# The reference tree: $METEOROS_REFERENCE, else a checkout named "reference"
+# beside this repository's directory.
+DEFAULT_REF = Path(os.environ.get("METEOROS_REFERENCE", ORACLE.parents[1] / "reference"))
 SHADERS = {
     "cloudRayMarch": "src/CloudScapes/shaders/cloudRayMarch.comp",
     "reprojection": "src/CloudScapes/shaders/reprojection.comp",

@@ -219,6 +219,23 @@ __attribute__((visibility("default"))) int ref_tonemap(const mt_time_ubo* tm, co
     return 0;
 }
 
+// The raymarch shader's helper functions, called one at a time:
+// getDensityHeightGradientForPoint (cloudRayMarch.comp:475-487; the shader
+// never calls it) and remap / remapClamped / remapClampedBeforeAndAfter
+// (:153-169).
+__attribute__((visibility("default"))) float ref_height_gradient(float h, float type) {
+    return glsl::sh_march::getDensityHeightGradientForPoint(h, type);
+}
+__attribute__((visibility("default"))) float ref_remap(float v, float a, float b, float c, float d) {
+    return glsl::sh_march::remap(v, a, b, c, d);
+}
+__attribute__((visibility("default"))) float ref_remap_clamped(float v, float a, float b, float c, float d) {
+    return glsl::sh_march::remapClamped(v, a, b, c, d);
+}
+__attribute__((visibility("default"))) float ref_remap_clamped_ba(float v, float a, float b, float c, float d) {
+    return glsl::sh_march::remapClampedBeforeAndAfter(v, a, b, c, d);
+}
+
 // WangHashNoise of postProcess_ToneMap.frag:52-66, as the shader computes it.
 __attribute__((visibility("default"))) float ref_wang_hash_noise(unsigned u, unsigned v, unsigned s) {
     return glsl::sh_tonemap::WangHashNoise(u, v, s);

@@ -34,8 +34,8 @@ The noise volumes fed to the shaders come from the seed-7 generator, with
 the base shape's R channel scaled by 0.8 (`golden_volumes`): under the
 reference's constants the unscaled volume gives a fully overcast sky, where
 every ray saturates and the god-ray mask is identically zero.  The run
-needs the reference tree (METEOROS_REFERENCE, default /root/reference); the
-tests only read the .npz.
+needs the reference tree ($METEOROS_REFERENCE, else a checkout named
+"reference" beside this repository); the tests only read the .npz.
 
 Usage: python tests/golden/make_golden.py
 """

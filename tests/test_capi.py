@@ -135,3 +135,35 @@ def test_create_without_gpu_reports_why(lib):
     assert st == abi.MT_ERR_UNSUPPORTED
     assert h.value is None
     assert lib.mt_last_error(None)
+
+
+def test_oracle_uniform_producers_equal_the_library(lib, oracle):
+    """The oracle's restatement of the reference's producers (used by the CPU
+    legs of the benchmark, which must not load the CUDA library) gives the
+    same bytes as the library's, so both arms render the same inputs."""
+    from meteoros_gb300 import scenes
+
+    def raw(s):
+        return bytes(C.string_at(C.addressof(s), C.sizeof(s)))
+
+    for i in range(0, 40):
+        for b in (2, 3, 5):
+            assert oracle.halton(i, b) == lib.mt_halton(i, b)
+    assert raw(oracle.time_init()) == raw(abi.time_init())
+    assert raw(oracle.params_reference()) == raw(abi.params_reference())
+    assert raw(oracle.params_config()) == raw(abi.params_config())
+    rng = np.random.default_rng(3)
+    for _ in range(200):
+        eye = tuple(float(x) for x in rng.uniform(-100, 100, 3))
+        ref = tuple(e + float(d) for e, d in zip(eye, rng.normal(size=3)))
+        fov, aspect = float(rng.uniform(20, 90)), float(rng.uniform(0.5, 3.0))
+        assert raw(oracle.camera_look_at(eye, ref, fov, aspect, 0.1, 1000.0)) == \
+            raw(abi.camera_look_at(eye, ref, fov, aspect, 0.1, 1000.0))
+    for seed in range(5):
+        a = scenes.config_sequence(seed, 1920, 1080, frames=4)
+        b = scenes.config_sequence(seed, 1920, 1080, frames=4, uniforms=oracle)
+        for fa, fb in zip(a, b):
+            assert all(raw(x) == raw(y) for x, y in zip(fa, fb))
+    a = scenes.reference_frame(64, 36, pitch_deg=10.0, frame=3, t=1.5)
+    b = scenes.reference_frame(64, 36, pitch_deg=10.0, frame=3, t=1.5, uniforms=oracle)
+    assert all(raw(x) == raw(y) for x, y in zip(a, b))

@@ -180,3 +180,65 @@ def test_tonemap_matches_reference_source(oracle, pyref, lib):
         a, _ = oracle.tonemap(t, img)
         b = pyref.tonemap(tm, img)
         assert_bit_exact(a, b, f"tone map t={t}")
+
+
+# ---- the CONFIG-only terms, against the reference's own functions ----
+
+def _grid_heights():
+    """Relative heights around every remap breakpoint of the gradient (0, 0.01,
+    0.1, 0.2, 0.25, 0.3, 0.6, 0.65, 0.95, 1) plus a dense sweep and out-of-range
+    values (the function clamps them)."""
+    h = [np.linspace(-0.5, 1.5, 4001, dtype=np.float32)]
+    for b in (0.0, 0.01, 0.1, 0.2, 0.25, 0.3, 0.6, 0.65, 0.95, 1.0):
+        c = np.float32(b)
+        h.append(np.array([np.nextafter(c, np.float32(-1)), c, np.nextafter(c, np.float32(2))], np.float32))
+    h.append(np.random.default_rng(31).random(20000, dtype=np.float32))
+    return np.concatenate(h)
+
+
+def test_height_gradient_matches_reference_source(oracle, pyref):
+    """getDensityHeightGradientForPoint (cloudRayMarch.comp:475-487) is dead
+    code in the reference; the CONFIG presets switch it on.  The oracle's
+    restatement equals the shader's own function bit for bit over heights x
+    cloud types (the weather map's B channel: every 8-bit value, as the
+    sampler sees it after filtering, and the configs' 0, 0.5, 1)."""
+    L = oracle.lib()
+    R = pyref.lib()
+    heights = _grid_heights()
+    types = np.concatenate([np.arange(256, dtype=np.float32) / np.float32(255.0),
+                            np.random.default_rng(32).random(64, dtype=np.float32),
+                            np.array([0.0, 0.5, 1.0, -0.25, 1.25], np.float32)])
+    mism = 0
+    for t in types:
+        a = np.array([L.orc_height_gradient(float(h), float(t)) for h in heights[::7]], np.float32)
+        b = np.array([R.ref_height_gradient(float(h), float(t)) for h in heights[::7]], np.float32)
+        mism += int((a.view(np.uint32) != b.view(np.uint32)).sum())
+    for t in (0.0, 0.5, 1.0):
+        a = np.array([L.orc_height_gradient(float(h), t) for h in heights], np.float32)
+        b = np.array([R.ref_height_gradient(float(h), t) for h in heights], np.float32)
+        mism += int((a.view(np.uint32) != b.view(np.uint32)).sum())
+        assert (b > 0).any()  # the gradient is not trivially zero on this grid
+    assert mism == 0, f"{mism} height-gradient values differ from the reference's function"
+
+
+def test_remaps_match_reference_source(oracle, pyref):
+    """remap / remapClamped / remapClampedBeforeAndAfter (cloudRayMarch.comp:153-169)
+    on the CONFIG preset's inputs: the base-shape remap (lo = fbm - 0.9), the
+    weather coverage remap (lo = 1 - R for every weather byte R) and the
+    erosion remap (lo = modifier * 0.005), plus random arguments."""
+    L = oracle.lib()
+    R = pyref.lib()
+    rng = np.random.default_rng(33)
+    vals = np.concatenate([rng.random(400, dtype=np.float32) * np.float32(1.4) - np.float32(0.2),
+                           np.array([0.0, 1.0, -0.0, 1e-30, 0.5], np.float32)])
+    los = np.concatenate([np.float32(1.0) - np.arange(256, dtype=np.float32) / np.float32(255.0),  # coverage
+                          rng.random(32, dtype=np.float32) - np.float32(0.9),  # base shape
+                          rng.random(32, dtype=np.float32) * np.float32(0.005)])  # erosion
+    cases = [(v, lo, 1.0, 0.0, 1.0) for lo in los for v in vals[::3]]
+    cases += [tuple(float(x) for x in rng.normal(size=5).astype(np.float32)) for _ in range(3000)]
+    for name in ("remap", "remap_clamped", "remap_clamped_ba"):
+        fa, fb = getattr(L, "orc_" + name), getattr(R, "ref_" + name)
+        a = np.array([fa(*map(float, c)) for c in cases], np.float32)
+        b = np.array([fb(*map(float, c)) for c in cases], np.float32)
+        same = (a.view(np.uint32) == b.view(np.uint32)) | (np.isnan(a) & np.isnan(b))
+        assert same.all(), f"{name}: {(~same).sum()} of {len(cases)} differ"
