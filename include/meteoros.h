@@ -317,15 +317,19 @@ MT_API mt_status mt_autotune_batch(mt_ctx* ctx, const mt_view* views, int n_view
  * counter live in one fixed device array of the library (about 0.7 MB):
  * at most MT_NOALLOC_MAX_VIEWS views and MT_NOALLOC_MAX_TILES tiles of the
  * context's batch tile shape; a batch beyond either limit is rejected with
- * MT_ERR_INVALID_ARG.  No CUDA graph is used: the tables are copied on
- * `stream`, then the reprojections and the persistent raymarch are launched
- * on it.  Results equal mt_render_batch.
+ * MT_ERR_INVALID_ARG before anything is launched.  Nothing is staged in
+ * host memory and the call never waits for the device: the view tables reach
+ * the array as the parameters of small store kernels launched on `stream`,
+ * the tile list is generated there by another kernel, then the reprojections
+ * and the persistent raymarch follow on the same stream.  Results equal
+ * mt_render_batch.
  *
  * The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress); make that first call before any stream capture.
- * Every call on a device shares the one array and leaves its tables there:
- * calls on one stream are ordered, but calls whose work may overlap on the
- * device (two streams not ordered by events) race on the array. */
+ * (cudaGetSymbolAddress, with that device current); make that first call
+ * before any stream capture.  Every call on a device shares the one array and
+ * leaves its tables there (the next call rewrites them and zeroes the work
+ * counter): calls on one stream are ordered, but calls whose work may overlap
+ * on the device (two streams not ordered by events) race on the array. */
 #define MT_NOALLOC_MAX_VIEWS 64
 #define MT_NOALLOC_MAX_TILES 32768
 MT_API mt_status mt_render_batch_noalloc(mt_ctx* ctx, const mt_view* views, int n_views, void* stream);

@@ -952,6 +952,13 @@ MT_API mt_status mt_get_kernel_times(mt_ctx* ctx, mt_kernel_times* out) {
 // fixed device array of this library instead of buffers the context
 // allocates.  Layout (bytes): [0, 256) work counter; [256, 256 + views)
 // MT_NOALLOC_MAX_VIEWS view tables; then MT_NOALLOC_MAX_TILES tiles.
+//
+// Nothing is staged in host memory: the view tables travel to the device as
+// the parameters of small store kernels (kNoallocStoreViews views a launch;
+// the launch copies its parameters, so nothing on the host is read after the
+// call returns), and the tile list is generated on the device from a small
+// per-view description, in the order mt_render_batch builds it on the host.
+// The call never waits for the device.
 namespace {
 
 constexpr size_t kNoallocViewsOff = 256;
@@ -961,23 +968,70 @@ constexpr size_t kNoallocTilesOff = kNoallocViewsOff + kNoallocViewsBytes;
 constexpr size_t kNoallocBytes = kNoallocTilesOff + MT_NOALLOC_MAX_TILES * sizeof(mt::BatchTile);
 constexpr int kNoallocMaxDevices = 64;
 static_assert(alignof(mt::MarchArgs) <= 256 && alignof(mt::BatchTile) <= 256, "scratch layout");
+static_assert(sizeof(mt::MarchArgs) % 4 == 0, "view tables are stored as 32-bit words");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
 
-// Host image of the array's counter + view region and its tile region,
-// filled under g_noalloc_mu and copied with cudaMemcpyAsync: a copy from
-// pageable memory is staged before the call returns, so the next call may
-// refill it at once.
-std::mutex g_noalloc_mu;
-unsigned char g_noalloc_host[kNoallocBytes];
+// Views per store launch: 16 view tables (~23 KB) stay inside the 32 KB of
+// kernel parameter space.
+constexpr int kNoallocStoreViews = 16;
+constexpr int kViewWords = (int)(sizeof(mt::MarchArgs) / 4);
+
+struct NoallocStore {
+    uint32_t words[kNoallocStoreViews * kViewWords];  // the view tables, as words
+    int32_t first_view, n_views;
+};
+static_assert(sizeof(NoallocStore) <= 32000, "kernel parameter space");
+
+// Copies n_views view tables into the array at view first_view; the launch
+// holding view 0 also zeroes the work counter.
+__global__ void noalloc_store_kernel(const __grid_constant__ NoallocStore p, unsigned char* scratch) {
+    uint32_t* dst = reinterpret_cast<uint32_t*>(scratch + kNoallocViewsOff) + (size_t)p.first_view * kViewWords;
+    const int n = p.n_views * kViewWords;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = p.words[i];
+    if (p.first_view == 0 && threadIdx.x == 0) *reinterpret_cast<unsigned*>(scratch) = 0u;
+}
+
+// The tile list's description: views in hand-out order with their ray grids
+// and the running tile count before each.
+struct NoallocTileSpec {
+    int32_t n_views, n_tiles, tile_w, tile_h;
+    int32_t view[MT_NOALLOC_MAX_VIEWS];
+    int32_t nx[MT_NOALLOC_MAX_VIEWS], ny[MT_NOALLOC_MAX_VIEWS];
+    int32_t bottom_up[MT_NOALLOC_MAX_VIEWS];
+    int32_t first[MT_NOALLOC_MAX_VIEWS + 1];
+};
+
+// Tile t of the list: the ordered view o with first[o] <= t < first[o + 1],
+// then its tile rows in march_row order, tw-wide tiles left to right in each
+// (the host loop of mt_render_batch, unrolled by index).
+__global__ void noalloc_tiles_kernel(const __grid_constant__ NoallocTileSpec p, unsigned char* scratch) {
+    mt::BatchTile* tiles = reinterpret_cast<mt::BatchTile*>(scratch + kNoallocTilesOff);
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < p.n_tiles; t += gridDim.x * blockDim.x) {
+        int lo = 0, hi = p.n_views - 1;  // last o with first[o] <= t
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) / 2;
+            if (p.first[mid] <= t) lo = mid; else hi = mid - 1;
+        }
+        const int o = lo, nx = p.nx[o], ny = p.ny[o];
+        const int ntx = (nx + p.tile_w - 1) / p.tile_w, nty = (ny + p.tile_h - 1) / p.tile_h;
+        const int local = t - p.first[o];
+        const int k = local / ntx, xi = local - k * ntx;
+        tiles[t] = mt::BatchTile{p.view[o], xi * p.tile_w, mt::march_row(k, nty, p.bottom_up[o] != 0) * p.tile_h,
+                                 nx, ny};
+    }
+}
+
+// Address of the array on each device, looked up (cudaGetSymbolAddress, with
+// the device current) on the first call made on that device.
+std::mutex g_noalloc_lookup_mu;
 unsigned char* g_noalloc_dev[kNoallocMaxDevices] = {};
 
-// Address of the array on ctx->device (current); looked up on the first
-// call made on that device.
 mt_status noalloc_scratch(mt_ctx* ctx, unsigned char** out) {
     if (ctx->device < 0 || ctx->device >= kNoallocMaxDevices)
         return fail(ctx, MT_ERR_UNSUPPORTED, "device %d is beyond the %d devices of the fixed scratch table",
                     ctx->device, kNoallocMaxDevices);
+    std::lock_guard<std::mutex> lk(g_noalloc_lookup_mu);
     if (!g_noalloc_dev[ctx->device]) {
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
@@ -1002,16 +1056,20 @@ MT_API mt_status mt_render_batch_noalloc(mt_ctx* ctx, const mt_view* views, int 
     if (n_views == 0) return MT_OK;
     mt_status st;
     if ((st = bind_device(ctx)) != MT_OK) return st;
-    std::lock_guard<std::mutex> lk(g_noalloc_mu);
     unsigned char* dev = nullptr;
     if ((st = noalloc_scratch(ctx, &dev)) != MT_OK) return st;
-    mt::MarchArgs* args = reinterpret_cast<mt::MarchArgs*>(g_noalloc_host + kNoallocViewsOff);
-    mt::BatchTile* tiles = reinterpret_cast<mt::BatchTile*>(g_noalloc_host + kNoallocTilesOff);
+    // Pass 1: validate every view and describe its ray grid, before anything
+    // is launched (a rejected batch leaves the array as it was).
+    NoallocTileSpec spec;
+    std::memset(&spec, 0, sizeof(spec));
+    mt::MarchArgs a;
+    double cost[MT_NOALLOC_MAX_VIEWS];
+    int nx[MT_NOALLOC_MAX_VIEWS], ny[MT_NOALLOC_MAX_VIEWS], bu[MT_NOALLOC_MAX_VIEWS], order[MT_NOALLOC_MAX_VIEWS];
     bool count = false;
     for (int i = 0; i < n_views; ++i) {
         const mt_view& v = views[i];
         st = build_march_args(ctx, &v.camera, &v.camera_old, &v.time, &v.params, v.prev_rgba, v.cur_rgba,
-                              v.godray_mask, v.width, v.height, v.flags, &args[i]);
+                              v.godray_mask, v.width, v.height, v.flags, &a);
         if (st != MT_OK) {
             const std::string m = ctx->err;
             return fail(ctx, st, "view %d: %s", i, m.c_str());
@@ -1019,15 +1077,10 @@ MT_API mt_status mt_render_batch_noalloc(mt_ctx* ctx, const mt_view* views, int 
         if (v.params.storage != views[0].params.storage)
             return fail(ctx, MT_ERR_INVALID_ARG, "view %d: all views of a batch must share one storage", i);
         count = count || (v.flags & MT_RENDER_COUNT);
-    }
-    // Tiles, most expensive views first (insertion sort of at most
-    // MT_NOALLOC_MAX_VIEWS views, stable like mt_render_batch's order).
-    int order[MT_NOALLOC_MAX_VIEWS];
-    double cost[MT_NOALLOC_MAX_VIEWS];
-    for (int i = 0; i < n_views; ++i) {
-        int nx, ny;
-        ray_grid(args[i], &nx, &ny);
-        cost[i] = (double)nx * ny * std::max(args[i].params.steps_min, args[i].params.steps_max);
+        ray_grid(a, &nx[i], &ny[i]);
+        bu[i] = a.bottom_up;
+        // most expensive views first, stable (mt_render_batch's order)
+        cost[i] = (double)nx[i] * ny[i] * std::max(a.params.steps_min, a.params.steps_max);
         int j = i;
         while (j > 0 && cost[order[j - 1]] < cost[i]) {
             order[j] = order[j - 1];
@@ -1038,36 +1091,47 @@ MT_API mt_status mt_render_batch_noalloc(mt_ctx* ctx, const mt_view* views, int 
     const int tw = ctx->batch_tile_w, th = ctx->batch_tile_h;
     long long n_tiles = 0;
     for (int o = 0; o < n_views; ++o) {
-        int nx, ny;
-        ray_grid(args[order[o]], &nx, &ny);
-        n_tiles += (long long)((nx + tw - 1) / tw) * ((ny + th - 1) / th);
+        const int i = order[o];
+        spec.view[o] = i;
+        spec.nx[o] = nx[i];
+        spec.ny[o] = ny[i];
+        spec.bottom_up[o] = bu[i];
+        spec.first[o] = (int32_t)std::min<long long>(n_tiles, MT_NOALLOC_MAX_TILES + 1);
+        n_tiles += (long long)((nx[i] + tw - 1) / tw) * ((ny[i] + th - 1) / th);
     }
     if (n_tiles > MT_NOALLOC_MAX_TILES)
         return fail(ctx, MT_ERR_INVALID_ARG,
                     "the batch needs %lld tiles of %dx%d rays; the fixed tile list holds %d", n_tiles, tw, th,
                     MT_NOALLOC_MAX_TILES);
-    long long t = 0;
-    for (int o = 0; o < n_views; ++o) {
-        const int i = order[o];
-        int nx, ny;
-        ray_grid(args[i], &nx, &ny);
-        const int nty = (ny + th - 1) / th;
-        for (int k = 0; k < nty; ++k) {
-            const int y = mt::march_row(k, nty, args[i].bottom_up != 0) * th;
-            for (int x = 0; x < nx; x += tw) tiles[t++] = mt::BatchTile{i, x, y, nx, ny};
-        }
-    }
-    // The work counter must start at zero: it is part of the first copy.
-    std::memset(g_noalloc_host, 0, kNoallocViewsOff);
+    spec.first[n_views] = (int32_t)n_tiles;
+    spec.n_views = n_views;
+    spec.n_tiles = (int32_t)n_tiles;
+    spec.tile_w = tw;
+    spec.tile_h = th;
+    // Pass 2: the view tables, kNoallocStoreViews views per store launch
+    // (the first launch also zeroes the work counter), then the tile list.
     cudaStream_t s = (cudaStream_t)stream;
-    MT_CUDA(ctx, cudaMemcpyAsync(dev, g_noalloc_host, kNoallocViewsOff + (size_t)n_views * sizeof(mt::MarchArgs),
-                                 cudaMemcpyHostToDevice, s));
-    if (n_tiles > 0)
-        MT_CUDA(ctx, cudaMemcpyAsync(dev + kNoallocTilesOff, tiles, (size_t)n_tiles * sizeof(mt::BatchTile),
-                                     cudaMemcpyHostToDevice, s));
-    for (int i = 0; i < n_views; ++i)
-        if (!(args[i].flags & MT_RENDER_FULL)) MT_CUDA(ctx, mt::launch_reproject(args[i], s));
+    NoallocStore store;
+    for (int v0 = 0; v0 < n_views; v0 += kNoallocStoreViews) {
+        store.first_view = v0;
+        store.n_views = std::min(kNoallocStoreViews, n_views - v0);
+        for (int k = 0; k < store.n_views; ++k) {
+            const mt_view& v = views[v0 + k];
+            build_march_args(ctx, &v.camera, &v.camera_old, &v.time, &v.params, v.prev_rgba, v.cur_rgba,
+                             v.godray_mask, v.width, v.height, v.flags, &a);  // validated above
+            std::memcpy(store.words + (size_t)k * kViewWords, &a, sizeof(a));
+            // the view's reprojection reads nothing of the array: launched as its table is built
+            if (!(a.flags & MT_RENDER_FULL)) MT_CUDA(ctx, mt::launch_reproject(a, s));
+        }
+        noalloc_store_kernel<<<1, 256, 0, s>>>(store, dev);
+        MT_CUDA(ctx, cudaGetLastError());
+    }
     if (n_tiles == 0) return MT_OK;
+    {
+        const int blocks = (int)std::min<long long>((n_tiles + 255) / 256, 128);
+        noalloc_tiles_kernel<<<blocks, 256, 0, s>>>(spec, dev);
+        MT_CUDA(ctx, cudaGetLastError());
+    }
     mt::BatchArgs b;
     b.views = reinterpret_cast<const mt::MarchArgs*>(dev + kNoallocViewsOff);
     b.tiles = reinterpret_cast<const mt::BatchTile*>(dev + kNoallocTilesOff);

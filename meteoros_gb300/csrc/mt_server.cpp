@@ -225,6 +225,15 @@ void worker_main(mt_server* s) {
     }
 }
 
+// Wait predicate of the calls that wait for a session's frame in flight.  The
+// session is looked up by key at every wake-up, never through an iterator kept
+// across the wait: the lock is released while waiting, and another caller may
+// close the session or insert into the map (a rehash invalidates iterators).
+bool session_idle_or_gone(mt_server* s, int64_t session) {
+    auto j = s->sessions.find(session);
+    return j == s->sessions.end() || !j->second.busy;
+}
+
 mt_status sfail(mt_server* s, mt_status st, const char* msg) {
     if (s) s->err = msg;
     return st;
@@ -345,11 +354,13 @@ MT_API mt_status mt_server_close_session(mt_server* s, int64_t session) {
     Session se;
     {
         std::unique_lock<std::mutex> lk(s->mu);
-        auto it = s->sessions.find(session);
-        if (it == s->sessions.end()) return sfail(s, MT_ERR_INVALID_ARG, "unknown session");
-        // wait (bounded) for the session's frame in flight
-        if (!s->cv_done.wait_for(lk, std::chrono::seconds(30), [&] { return !it->second.busy; }))
+        if (s->sessions.find(session) == s->sessions.end()) return sfail(s, MT_ERR_INVALID_ARG, "unknown session");
+        // wait (bounded) for the session's frame in flight, or for another
+        // caller to close it meanwhile
+        if (!s->cv_done.wait_for(lk, std::chrono::seconds(30), [&] { return session_idle_or_gone(s, session); }))
             return sfail(s, MT_ERR_TIMEOUT, "session still busy");
+        auto it = s->sessions.find(session);
+        if (it == s->sessions.end()) return sfail(s, MT_ERR_INVALID_ARG, "session closed meanwhile");
         se = it->second;
         s->sessions.erase(it);
     }
@@ -391,11 +402,17 @@ MT_API mt_status mt_server_submit(mt_server* s, int64_t session, const mt_camera
 MT_API mt_status mt_server_wait(mt_server* s, uint64_t request, int timeout_ms, mt_request_info* out) {
     if (!s) return MT_ERR_INVALID_ARG;
     std::unique_lock<std::mutex> lk(s->mu);
-    auto it = s->requests.find(request);
-    if (it == s->requests.end()) return sfail(s, MT_ERR_INVALID_ARG, "unknown request");
-    if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(std::max(0, timeout_ms)),
-                             [&] { return it->second.done; }))
+    if (s->requests.find(request) == s->requests.end()) return sfail(s, MT_ERR_INVALID_ARG, "unknown request");
+    // looked up again at every wake-up: another waiter may have taken the
+    // request, and inserts may rehash the map (both invalidate iterators)
+    const auto done_or_gone = [&] {
+        auto j = s->requests.find(request);
+        return j == s->requests.end() || j->second.done;
+    };
+    if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(std::max(0, timeout_ms)), done_or_gone))
         return MT_ERR_TIMEOUT;
+    auto it = s->requests.find(request);
+    if (it == s->requests.end()) return sfail(s, MT_ERR_INVALID_ARG, "request taken by another waiter");
     const Request& r = it->second;
     if (out) {
         out->id = r.id;
@@ -418,10 +435,11 @@ MT_API mt_status mt_server_read_frame(mt_server* s, int64_t session, float* host
     size_t px = 0;
     {
         std::unique_lock<std::mutex> lk(s->mu);
-        auto it = s->sessions.find(session);
-        if (it == s->sessions.end()) return sfail(s, MT_ERR_INVALID_ARG, "unknown session");
-        if (!s->cv_done.wait_for(lk, std::chrono::seconds(30), [&] { return !it->second.busy; }))
+        if (s->sessions.find(session) == s->sessions.end()) return sfail(s, MT_ERR_INVALID_ARG, "unknown session");
+        if (!s->cv_done.wait_for(lk, std::chrono::seconds(30), [&] { return session_idle_or_gone(s, session); }))
             return sfail(s, MT_ERR_TIMEOUT, "session still busy");
+        auto it = s->sessions.find(session);
+        if (it == s->sessions.end()) return sfail(s, MT_ERR_INVALID_ARG, "session closed meanwhile");
         Session& se = it->second;
         if (!se.has_prev) return sfail(s, MT_ERR_NO_VOLUMES, "session has no frame yet");
         se.busy = true;  // no frame of the session starts while it is read

@@ -23,6 +23,17 @@ oracle/ref_build.py from the reference tree -- on seeded synthetic inputs:
                           from "<name>(z+1).tga", ImageLoadingUtility.cpp:75-139)
   gen_sha256_*            SHA-256 of the seed-7 generator volumes (pins the
                           generator bit for bit across hosts)
+  ref_assets.npz          (a file of its own) REF-preset frames on volumes built
+                          from the reference's shipped noise assets, for the
+                          GPU test, which has no reference tree: the TGA bytes
+                          of all 32 HighFrequency slices and of LowFrequency
+                          slices 1-2 (the base stack repeats them 64 times:
+                          the whole 128-slice stack is 8.4 MB of noise that no
+                          compressor shrinks), curlNoise.png as stb_image
+                          decodes it, SHA-256 of the two volumes as stb_image
+                          decodes the stacks, and for each view the uniform
+                          bytes plus the reference shaders' checkerboard frame
+                          and god-ray mask
   *_ubo                   the exact uniform-block bytes every golden was made
                           with: cameras are built with tan/sin/cos of the host's
                           libm, which may differ by an ulp between hosts, and an
@@ -54,6 +65,11 @@ from meteoros_gb300 import abi, build, scenes  # noqa: E402
 from oracle import pyoracle, pyref  # noqa: E402
 
 OUT = Path(__file__).resolve().parent / "golden.npz"
+OUT_ASSETS = Path(__file__).resolve().parent / "ref_assets.npz"
+ASSET_LOW_SLICES = 2  # LowFrequency(1..2).tga, stacked 64 times into the 128-slice base volume
+ASSET_W, ASSET_H = 64, 36
+# (yaw, pitch, checkerboard slot, time.y) of the REF frames on the shipped assets
+ASSET_VIEWS = ((0.0, 8.0, 3, 3.5), (35.0, 22.0, 12, 17.25), (-60.0, 4.0, 9, 0.0))
 
 SEQ_W, SEQ_H, SEQ_PITCH = 64, 36, 20.0
 QUIRK_W, QUIRK_H, QUIRK_FRAME = 130, 18, 5
@@ -132,6 +148,50 @@ def mg_textures() -> Path:
     return ref_build.DEFAULT_REF / "src/CloudScapes/textures/CloudTextures"
 
 
+def asset_stack_order():
+    """Shipped slice file of each base-volume slice z: LowFrequency((z % 2) + 1)."""
+    return [z % ASSET_LOW_SLICES for z in range(abi.MT_BASE_N)]
+
+
+def asset_prev(k: int):
+    return np.random.default_rng(40 + k).random((ASSET_H, ASSET_W, 4), dtype=np.float32)
+
+
+def unpack_files(blob: np.ndarray, offsets: np.ndarray) -> list[bytes]:
+    raw = bytes(np.asarray(blob, np.uint8))
+    return [raw[int(a):int(b)] for a, b in zip(offsets[:-1], offsets[1:])]
+
+
+def make_ref_assets() -> dict:
+    """The fixture of REF frames on volumes from the shipped assets (see the module docstring)."""
+    tex = mg_textures()
+    low = [(tex / "LowFrequency" / f"LowFrequency({z + 1}).tga").read_bytes() for z in range(ASSET_LOW_SLICES)]
+    high = [(tex / "HighFrequency" / f"HighFrequency({z + 1}).tga").read_bytes() for z in range(abi.MT_DETAIL_N)]
+    out = {}
+    for key, files in (("low", low), ("high", high)):
+        out[f"{key}_tga"] = np.frombuffer(b"".join(files), np.uint8).copy()
+        out[f"{key}_offsets"] = np.cumsum([0] + [len(f) for f in files]).astype(np.int64)
+    low_dec = [pyref.stbi_load_rgba(f) for f in low]
+    base = np.stack([low_dec[i] for i in asset_stack_order()])
+    detail = np.stack([pyref.stbi_load_rgba(f) for f in high])
+    curl = pyref.stbi_load_rgba((tex / "curlNoise.png").read_bytes())
+    weather = np.zeros((abi.MT_WEATHER_N, abi.MT_WEATHER_N, 4), np.uint8)  # the REF preset never reads it
+    out["curl_rgba8"] = curl
+    out["base_sha256"] = np.frombuffer(hashlib.sha256(base.tobytes()).digest(), np.uint8)
+    out["detail_sha256"] = np.frombuffer(hashlib.sha256(detail.tobytes()).digest(), np.uint8)
+    vol = pyoracle.Volumes(base, detail, curl, weather)
+    for k, (yaw, pitch, slot, t) in enumerate(ASSET_VIEWS):
+        cam = scenes.look((0.0, 0.0, 2.0), yaw, pitch, 45.0, ASSET_W, ASSET_H)
+        old = scenes.look((0.0, 0.0, 2.0), yaw - 0.25, pitch, 45.0, ASSET_W, ASSET_H)
+        tm = abi.time_init()
+        tm.frame_count_mod16 = slot
+        tm.time[0] = 0.016
+        tm.time[1] = t
+        out[f"view{k}_ubo"] = ubo_bytes(cam, old, tm)
+        out[f"view{k}_rgba"], out[f"view{k}_mask"] = pyref.frame(vol, cam, old, tm, asset_prev(k), ASSET_W, ASSET_H)
+    return out
+
+
 def main() -> int:
     build.build()
     if not pyref.available():
@@ -179,6 +239,8 @@ def main() -> int:
                 hashlib.sha256(np.ascontiguousarray(v[k + suffix]).tobytes()).digest(), np.uint8)
     np.savez_compressed(OUT, **out)
     print(f"wrote {OUT} ({OUT.stat().st_size} bytes)")
+    np.savez_compressed(OUT_ASSETS, **make_ref_assets())
+    print(f"wrote {OUT_ASSETS} ({OUT_ASSETS.stat().st_size} bytes)")
     return 0
 
 

@@ -401,3 +401,37 @@ def test_fused_frame_equals_render_then_txaa(ctx, size):
             ctx.render(cam, cam_old, tm, params, prev, cur_c, None, flags)
             assert_bits_equal(cur_c.cpu().numpy(), cur_a.cpu().numpy(), what + " mt_render")
         ctx.set_tuning(fused_resolve=False, reproject_serial=False)
+
+
+def test_config1_chain_16_frames(ctx, oracle, vol7):
+    """A 16-frame config-1 sequence at 480x270 through Session (the
+    reference's ping-pong, Renderer.cpp:131-136, 191): each frame reprojects
+    the previous raw frame and TXAA resolves against the previous resolved
+    frame, the GPU and the oracle each fed their own outputs, checked frame by
+    frame (raw and resolved colour within the HDR bar, marched god-ray values
+    bit-exact, executed-sample counters exact)."""
+    from meteoros_gb300.renderer import FrameInputs, Session
+
+    w, h = 480, 270
+    seq = scenes.config_sequence(2017, w, h, frames=16)
+    sess = Session(ctx, w, h, txaa=True)
+    ctx.stats(reset=True)
+    raw = out = None
+    for k, (cam, old, tm, params) in enumerate(seq):
+        sess.frame(FrameInputs(cam, old, tm, params), flags=abi.MT_RENDER_CHECKERBOARD | abi.MT_RENDER_COUNT)
+        torch.cuda.synchronize()
+        st = ctx.stats(reset=True)
+        if k == 0:
+            raw, mask, cnt = oracle.render(vol7, cam, old, tm, params, None, w, h, abi.MT_RENDER_FULL)
+            out = oracle.txaa(cam, old, tm, params, raw, raw)
+        else:
+            raw, mask, cnt = oracle.render(vol7, cam, old, tm, params, raw, w, h, 0)
+            out = oracle.txaa(cam, old, tm, params, raw, out)
+        g_raw = sess.raw[sess.parity ^ 1].cpu().numpy()
+        assert_hdr_close(g_raw, raw, f"frame {k} raw")
+        assert_hdr_close(sess.output.cpu().numpy(), out, f"frame {k} resolved")
+        m = ~np.isnan(mask)
+        sx, sy = params.slot_x[tm.frame_count_mod16], params.slot_y[tm.frame_count_mod16]
+        assert m.sum() == (w * h if k == 0 else ((w - sx + 3) // 4) * ((h - sy + 3) // 4))
+        assert_bits_equal(sess.mask.cpu().numpy()[m], mask[m], f"frame {k} god-ray values")
+        assert (st.primary_samples, st.light_samples, st.marched_rays) == (int(cnt[0]), int(cnt[1]), int(cnt[2])), k

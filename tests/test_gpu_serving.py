@@ -180,3 +180,73 @@ def test_admission_waits_for_budget_to_free(ctx):
         with pytest.raises(abi.MeteorosError) as e:
             srv.open_session(320, 180, params)
         assert e.value.status == abi.MT_ERR_BUDGET
+
+
+def test_concurrent_close_read_and_wait(ctx):
+    """Several host threads close, read and wait on the same sessions and
+    requests at once while others open sessions (inserts that rehash the
+    server's maps): every call returns a defined status -- one close of a
+    session succeeds, the others report an unknown or meanwhile-closed
+    session; one wait on a request takes it, the other reports it unknown."""
+    import ctypes as C
+    import threading
+
+    from meteoros_gb300.server import Server
+
+    lib = ctx.lib
+    _, _, params, _ = scenes.config_view(5, 160, 90)
+    for rnd in range(4):
+        with Server(ctx, max_batch=8, streams=2, hbm_budget_bytes=1 << 30) as srv:
+            h = srv.handle
+            sids = [srv.open_session(160, 90, params) for _ in range(12)]
+            path = session_path(rnd, 160, 90, 1)[0]
+            rids = [srv.submit(s, *path[0]) for s in sids]
+            results = {"close": [], "read": [], "wait": [], "open": []}
+            lock = threading.Lock()
+            rgba = np.empty((90, 160, 4), np.float32)
+
+            def close(s):
+                st = lib.mt_server_close_session(h, C.c_int64(s))
+                with lock:
+                    results["close"].append((s, st))
+
+            def read(s):
+                buf = np.empty_like(rgba)
+                st = lib.mt_server_read_frame(h, C.c_int64(s), buf.ctypes.data_as(C.c_void_p), None)
+                with lock:
+                    results["read"].append((s, st))
+
+            def wait(r):
+                info = abi.RequestInfo()
+                st = lib.mt_server_wait(h, C.c_uint64(r), 30000, C.byref(info))
+                with lock:
+                    results["wait"].append((r, st))
+
+            def opener():
+                for _ in range(64):  # grows the session map past several rehashes
+                    sid = C.c_int64()
+                    st = lib.mt_server_open_session(h, 16, 16, C.byref(params), C.byref(sid))
+                    with lock:
+                        results["open"].append(st)
+
+            threads = [threading.Thread(target=opener)]
+            for s, r in zip(sids, rids):
+                threads += [threading.Thread(target=wait, args=(r,)), threading.Thread(target=wait, args=(r,)),
+                            threading.Thread(target=read, args=(s,)), threading.Thread(target=close, args=(s,)),
+                            threading.Thread(target=close, args=(s,))]
+            for t in threads:
+                t.start()
+            for t in threads:
+                t.join(60)
+            assert not any(t.is_alive() for t in threads)
+            assert all(st == abi.MT_OK for st in results["open"])
+            for s in sids:
+                sts = sorted(st for x, st in results["close"] if x == s)
+                assert sts == [abi.MT_OK, abi.MT_ERR_INVALID_ARG], (s, sts)
+            for s, st in results["read"]:
+                assert st in (abi.MT_OK, abi.MT_ERR_INVALID_ARG, abi.MT_ERR_NO_VOLUMES), (s, st)
+            for r in rids:
+                sts = sorted(st for x, st in results["wait"] if x == r)
+                # the request may be failed (INVALID_ARG) when its session closed before it ran
+                assert sts.count(abi.MT_ERR_INVALID_ARG) >= 1 and len(sts) == 2, (r, sts)
+                assert all(st in (abi.MT_OK, abi.MT_ERR_INVALID_ARG) for st in sts), (r, sts)

@@ -1,7 +1,8 @@
 """mt_render_batch_noalloc against mt_render_batch, through the C ABI (GB300 only).
 
 The allocation-free entry point keeps its view table, tile list and work
-counter in one fixed device array of the library.  Two calls in a row (a
+counter in one fixed device array of the library, for callers that cannot
+allocate device memory on their render path.  Two calls in a row (a
 different batch each time, so the second runs over the first one's leftover
 tables) must each give what mt_render_batch gives for the same views.  This
 file is collected last so that it runs both after the other GPU tests and,
@@ -28,7 +29,7 @@ def ctx(lib):
 
     c = Context(0)
     c.generate_volumes(7)
-    for v in range(12):
+    for v in range(40):
         c.generate_weather(v, 7 + v)
     yield c
     c.close()
@@ -74,7 +75,8 @@ def run(ctx, name, views, imgs):
 
 def test_noalloc_equals_render_batch_on_two_calls_in_a_row(ctx):
     ctx.stats(reset=True)
-    for seed, n_views, storage in ((11, 12, abi.MT_STORAGE_U8), (12, 7, abi.MT_STORAGE_F16)):
+    # 40 views: three store launches of the view tables; then 7 over their leftovers
+    for seed, n_views, storage in ((11, 40, abi.MT_STORAGE_U8), (12, 7, abi.MT_STORAGE_F16)):
         views, imgs = make_batch(seed, n_views, storage)
         want, st_want = run(ctx, "mt_render_batch", views, imgs)
         got, st_got = run(ctx, "mt_render_batch_noalloc", views, imgs)
