@@ -9,6 +9,9 @@ per-frame inputs are synthetic and seeded.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
+With --gpus N > 1 and no launcher environment (WORLD_SIZE unset) the script
+runs itself as N ranks under torch.distributed.run on this node.
+
 Timing: W untimed warm-up frames, then K frames; before each frame a 256 MiB
 buffer is written to flush L2 (outside the frame's events); each frame is
 bracketed by CUDA events on the launching stream.  The same K frames then run
@@ -336,19 +339,47 @@ def bench_precision(ctx, torch, flush, reps: int = 3, err_stride: int = 16) -> d
                          reps)
         ent = {"ms": round(ms, 3), "gsamples_per_s": round(samples / (ms * 1e-3) / 1e9, 3)}
         if ref_vols is not None:
-            ref, _ = pyoracle.march_pixels(ref_vols[name], cam, tm, p, W, H, xy, dtype=np.float64)
+            # the error pass: one traced render (same pixels as the timed
+            # ones), each ray's control flow beside the FP64 oracle's
+            trace = torch.zeros((H, W, 4), dtype=torch.int32, device="cuda")
+            ctx.set_sample_trace(trace)
+            ctx.render(cam, cam, tm, p, None, cur, mask, abi.MT_RENDER_FULL)
+            ctx.set_sample_trace(None)
+            ref, _, ref_tr = pyoracle.march_pixels(ref_vols[name], cam, tm, p, W, H, xy, dtype=np.float64,
+                                                   counts=True)
             got = cur.cpu().numpy()[xy[:, 1], xy[:, 0], :3].astype(np.float64)
-            r = ref[:, :3]
-            d = np.abs(got - r).max(-1)
-            bright = np.abs(r).max(-1) > 4096.0  # the sun disk: held to relative error
-            dn = d[~bright]
-            rel = (d[bright] / np.abs(r[bright]).max(-1)) if bright.any() else np.zeros(1)
-            ent["err_vs_fp64"] = {"max_abs": float(dn.max()), "mean_abs": float(dn.mean()),
-                                  "p99_abs": float(np.percentile(dn, 99)),
-                                  "frac_le_2e-3": float((dn <= 2e-3).mean()),
-                                  "bright_pixels": int(bright.sum()), "bright_max_rel": float(rel.max()),
-                                  "pixels": int(d.size)}
+            got_tr = trace.cpu().numpy().view(np.uint32)[xy[:, 1], xy[:, 0]]
+            same = (got_tr == ref_tr).all(1)
+            ent["err_vs_fp64"] = precision_error(got, ref[:, :3], same)
         out[name] = ent
+    return out
+
+
+def precision_error(got, ref, same) -> dict:
+    """Error of a frame sample against the FP64 oracle.  `same`: the pixels
+    whose march took the same branch at every threshold as the oracle's (equal
+    step counts and control-flow signatures); the others flipped a threshold
+    (a step in or out of cloud, a light sample's cbl > 0, a jitter index or the
+    early exit), which moves the colour by a whole step's contribution.
+    Pixels brighter than 4096 (the sun disk) are held to relative error."""
+    import numpy as np
+
+    d = np.abs(got - ref).max(-1)
+    bright = np.abs(ref).max(-1) > 4096.0
+    rel = (d[bright] / np.abs(ref[bright]).max(-1)) if bright.any() else np.zeros(1)
+    dn, dk = d[~bright], d[same & ~bright]
+    out = {"max_abs": float(dn.max()), "mean_abs": float(dn.mean()), "p99_abs": float(np.percentile(dn, 99)),
+           "frac_le_2e-3": float((dn <= 2e-3).mean()), "bright_pixels": int(bright.sum()),
+           "bright_max_rel": float(rel.max()), "pixels": int(d.size),
+           "flip_frac": float(1.0 - same.mean())}
+    if dk.size:
+        # relative to max(1, |value|): absolute below 1, relative above
+        rk = (d / np.maximum(1.0, np.abs(ref).max(-1)))[same & ~bright]
+        out["same_branches"] = {"pixels": int(dk.size), "max_abs": float(dk.max()), "mean_abs": float(dk.mean()),
+                                "p99_abs": float(np.percentile(dk, 99)), "p999_abs": float(np.percentile(dk, 99.9)),
+                                "frac_le_2e-3": float((dk <= 2e-3).mean()), "max_rel": float(rk.max()),
+                                "p999_rel": float(np.percentile(rk, 99.9)),
+                                "frac_rel_le_2e-3": float((rk <= 2e-3).mean())}
     return out
 
 
@@ -662,8 +693,24 @@ def run_gb300(args) -> int:
     return 0
 
 
+def launch_ranks(n: int) -> int:
+    """`--gpus N` without a launcher: run this same command as N ranks under
+    torch.distributed.run on this node (rendezvous on 127.0.0.1), one replica
+    per GPU; rank 0 prints the line."""
+    import socket
+
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes", "1", "--nproc-per-node", str(n),
+           "--master-addr", "127.0.0.1", "--master-port", str(port), str(Path(__file__).resolve()), *sys.argv[1:]]
+    return subprocess.call(cmd)
+
+
 def main() -> int:
     args = parse()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        return launch_ranks(args.gpus)
     if args.impl == "reference":
         return run_reference(args)
     return run_gb300(args)

@@ -303,6 +303,21 @@ MT_API mt_status mt_txaa(mt_ctx* ctx, const mt_camera_ubo* camera, const mt_came
  * flight together must not overlap. */
 MT_API mt_status mt_render_batch(mt_ctx* ctx, const mt_view* views, int n_views, void* stream);
 
+/* Diagnostic, no counterpart in the reference: while `counts` is not NULL,
+ * every mt_render / mt_render_frame of this context writes, for each marched
+ * pixel (x, y), four uint32 at counts[4 * (y * width + x)]: the ray's executed
+ * primary samples, its in-cloud samples (density > 0,
+ * cloudRayMarch.comp:642), its control-flow signature and 0.  The signature
+ * is an FNV-1a hash (offset 2166136261, prime 16777619) over the executed
+ * steps, in order, of (jitter index | in cloud << 4 | light sample i's
+ * cbl > 0 << (5 + i)); 0 for a ray that marched no step.  `counts` is a
+ * 16-byte-aligned device buffer of width x height x 4 uint32 the caller owns,
+ * for the size of the frames rendered.  It records each ray's control flow,
+ * e.g. to tell pixels whose march took the same branches as an oracle's from
+ * pixels where a threshold flipped.  NULL turns it off.  Traced renders use
+ * 1 or 4 lanes per ray and 256-thread CTAs; batched renders never write it. */
+MT_API mt_status mt_set_sample_trace(mt_ctx* ctx, void* counts);
+
 /* Times mt_render_batch on these views for every tile shape in
  * {8x8, 16x8, 16x16, 32x8} and lanes in {1, 4}, keeps the fastest in the
  * context's tuning and returns it (the views are rendered several times). */

@@ -183,6 +183,7 @@ SIGNATURES = {
     "mt_txaa": (C.c_int, [_P, C.POINTER(CameraUBO), C.POINTER(CameraUBO), C.POINTER(TimeUBO),
                           C.POINTER(Params), _P, _P, _P, C.c_int, C.c_int, _P]),
     "mt_render_batch": (C.c_int, [_P, C.POINTER(View), C.c_int, _P]),
+    "mt_set_sample_trace": (C.c_int, [_P, _P]),
     "mt_get_stats": (C.c_int, [_P, C.POINTER(Stats), C.c_int, _P]),
     "mt_autotune_batch": (C.c_int, [_P, C.POINTER(View), C.c_int, _P, C.POINTER(Tuning)]),
     "mt_render_batch_noalloc": (C.c_int, [_P, C.POINTER(View), C.c_int, _P]),

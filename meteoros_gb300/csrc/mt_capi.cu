@@ -32,6 +32,11 @@ struct mt_ctx {
     uint2* curl16[2] = {nullptr, nullptr};
     std::vector<uint32_t*> weather;           // MT_MAX_WEATHER_SLOTS entries, allocated on demand
     std::vector<uint2*> weather16[2];
+    // filter-cell copies of the RGBA8 volumes (the plain form's samplers read these)
+    uint4* base_c = nullptr;                  // MT_BASE_N^3 x 2
+    uint4* detail_c = nullptr;                // MT_DETAIL_N^3 x 2
+    uint4* curl_c = nullptr;                  // MT_CURL_N^2
+    std::vector<uint4*> weather_c;            // MT_WEATHER_N^2 per slot
     bool have_base = false, have_detail = false, have_curl = false;
     unsigned long long* stats = nullptr;      // 4 counters
     bool timing = false;
@@ -61,6 +66,7 @@ struct mt_ctx {
     cudaStream_t aux = nullptr;
     cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     int overlap = 1;
+    uint4* trace = nullptr;                   // mt_set_sample_trace
 };
 
 namespace {
@@ -143,6 +149,8 @@ mt_status ensure_weather(mt_ctx* ctx, int slot) {
     if (st != MT_OK) return st;
     st = alloc(ctx, &ctx->weather16[0][slot], kWeatherTexels);
     if (st != MT_OK) return st;
+    st = alloc(ctx, &ctx->weather_c[slot], kWeatherTexels);
+    if (st != MT_OK) return st;
     return alloc(ctx, &ctx->weather16[1][slot], kWeatherTexels);
 }
 
@@ -151,6 +159,9 @@ mt_status ensure_volumes(mt_ctx* ctx) {
     if ((st = alloc(ctx, &ctx->base, kBaseTexels)) != MT_OK) return st;
     if ((st = alloc(ctx, &ctx->detail, kDetailTexels)) != MT_OK) return st;
     if ((st = alloc(ctx, &ctx->curl, kCurlTexels)) != MT_OK) return st;
+    if ((st = alloc(ctx, &ctx->base_c, 2 * kBaseTexels)) != MT_OK) return st;
+    if ((st = alloc(ctx, &ctx->detail_c, 2 * kDetailTexels)) != MT_OK) return st;
+    if ((st = alloc(ctx, &ctx->curl_c, kCurlTexels)) != MT_OK) return st;
     for (int k = 0; k < 2; ++k) {
         if ((st = alloc(ctx, &ctx->base16[k], kBaseTexels)) != MT_OK) return st;
         if ((st = alloc(ctx, &ctx->detail16[k], kDetailTexels)) != MT_OK) return st;
@@ -185,12 +196,12 @@ mt_status build_march_args(mt_ctx* ctx, const mt_camera_ubo* cam, const mt_camer
     a->time = *tm;
     a->params = *p;
     const int k = p->storage == MT_STORAGE_BF16 ? 1 : 0;
-    const uint32_t* weather8 = (p->coverage_mode == 1) ? ctx->weather[p->weather_slot] : ctx->curl;
+    const uint4* weather8 = (p->coverage_mode == 1) ? ctx->weather_c[p->weather_slot] : ctx->curl_c;
     const uint2* weather16 = (p->coverage_mode == 1) ? ctx->weather16[k][p->weather_slot] : ctx->curl16[k];
     if (p->storage == MT_STORAGE_U8) {
-        a->vol[0] = ctx->base;
-        a->vol[1] = ctx->detail;
-        a->vol[2] = ctx->curl;
+        a->vol[0] = ctx->base_c;
+        a->vol[1] = ctx->detail_c;
+        a->vol[2] = ctx->curl_c;
         a->vol[3] = weather8;  // never read when coverage_mode == 0
     } else {
         a->vol[0] = ctx->base16[k];
@@ -249,6 +260,7 @@ MT_API mt_status mt_create(mt_ctx** out, int device) {
     if (!ctx) return fail(nullptr, MT_ERR_OUT_OF_MEMORY, "host allocation failed");
     ctx->device = device;
     ctx->weather.assign(MT_MAX_WEATHER_SLOTS, nullptr);
+    ctx->weather_c.assign(MT_MAX_WEATHER_SLOTS, nullptr);
     ctx->weather16[0].assign(MT_MAX_WEATHER_SLOTS, nullptr);
     ctx->weather16[1].assign(MT_MAX_WEATHER_SLOTS, nullptr);
     if (bind_device(ctx) != MT_OK || alloc(ctx, &ctx->stats, 4) != MT_OK ||
@@ -270,6 +282,10 @@ MT_API void mt_destroy(mt_ctx* ctx) {
     cudaFree(ctx->base);
     cudaFree(ctx->detail);
     cudaFree(ctx->curl);
+    cudaFree(ctx->base_c);
+    cudaFree(ctx->detail_c);
+    cudaFree(ctx->curl_c);
+    for (uint4* w : ctx->weather_c) cudaFree(w);
     for (int k = 0; k < 2; ++k) {
         cudaFree(ctx->base16[k]);
         cudaFree(ctx->detail16[k]);
@@ -311,16 +327,19 @@ MT_API mt_status mt_upload_volumes(mt_ctx* ctx, const uint8_t* base, const uint8
     if (base) {
         MT_CUDA(ctx, cudaMemcpy(ctx->base, base, kBaseTexels * 4, cudaMemcpyHostToDevice));
         MT_CUDA(ctx, mt::launch_u8_to_16(ctx->base, kBaseTexels, ctx->base16[0], ctx->base16[1], 0));
+        MT_CUDA(ctx, mt::launch_cells3(ctx->base, MT_BASE_N, ctx->base_c, 0));
         ctx->have_base = true;
     }
     if (detail) {
         MT_CUDA(ctx, cudaMemcpy(ctx->detail, detail, kDetailTexels * 4, cudaMemcpyHostToDevice));
         MT_CUDA(ctx, mt::launch_u8_to_16(ctx->detail, kDetailTexels, ctx->detail16[0], ctx->detail16[1], 0));
+        MT_CUDA(ctx, mt::launch_cells3(ctx->detail, MT_DETAIL_N, ctx->detail_c, 0));
         ctx->have_detail = true;
     }
     if (curl) {
         MT_CUDA(ctx, cudaMemcpy(ctx->curl, curl, kCurlTexels * 4, cudaMemcpyHostToDevice));
         MT_CUDA(ctx, mt::launch_u8_to_16(ctx->curl, kCurlTexels, ctx->curl16[0], ctx->curl16[1], 0));
+        MT_CUDA(ctx, mt::launch_cells2(ctx->curl, MT_CURL_N, ctx->curl_c, 0));
         ctx->have_curl = true;
     }
     if (weather) {
@@ -377,6 +396,7 @@ MT_API mt_status mt_decode_tga_volume(mt_ctx* ctx, int volume, const uint8_t* co
     if (e == cudaSuccess)
         e = mt::launch_u8_to_16(vol, texels, volume == MT_VOLUME_BASE ? ctx->base16[0] : ctx->detail16[0],
                                 volume == MT_VOLUME_BASE ? ctx->base16[1] : ctx->detail16[1], s);
+    if (e == cudaSuccess) e = mt::launch_cells3(vol, n, volume == MT_VOLUME_BASE ? ctx->base_c : ctx->detail_c, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     cudaFree(d_blob);
     cudaFree(d_table);
@@ -400,6 +420,7 @@ MT_API mt_status mt_upload_weather(mt_ctx* ctx, int slot, const uint8_t* weather
     MT_CUDA(ctx, cudaMemcpy(ctx->weather[slot], weather, kWeatherTexels * 4, cudaMemcpyHostToDevice));
     MT_CUDA(ctx, mt::launch_u8_to_16(ctx->weather[slot], kWeatherTexels, ctx->weather16[0][slot],
                                      ctx->weather16[1][slot], 0));
+    MT_CUDA(ctx, mt::launch_cells2(ctx->weather[slot], MT_WEATHER_N, ctx->weather_c[slot], 0));
     MT_CUDA(ctx, cudaDeviceSynchronize());
     return MT_OK;
 }
@@ -414,6 +435,9 @@ MT_API mt_status mt_generate_volumes(mt_ctx* ctx, uint64_t seed, void* stream) {
     MT_CUDA(ctx, mt::launch_generate_base(s32, mt::NoiseOut{ctx->base, ctx->base16[0], ctx->base16[1]}, s));
     MT_CUDA(ctx, mt::launch_generate_detail(s32, mt::NoiseOut{ctx->detail, ctx->detail16[0], ctx->detail16[1]}, s));
     MT_CUDA(ctx, mt::launch_generate_curl(s32, mt::NoiseOut{ctx->curl, ctx->curl16[0], ctx->curl16[1]}, s));
+    MT_CUDA(ctx, mt::launch_cells3(ctx->base, MT_BASE_N, ctx->base_c, s));
+    MT_CUDA(ctx, mt::launch_cells3(ctx->detail, MT_DETAIL_N, ctx->detail_c, s));
+    MT_CUDA(ctx, mt::launch_cells2(ctx->curl, MT_CURL_N, ctx->curl_c, s));
     ctx->have_base = ctx->have_detail = ctx->have_curl = true;
     return mt_generate_weather(ctx, 0, seed, stream);
 }
@@ -427,6 +451,7 @@ MT_API mt_status mt_generate_weather(mt_ctx* ctx, int slot, uint64_t seed, void*
     MT_CUDA(ctx, mt::launch_generate_weather(
                      seed32(seed), mt::NoiseOut{ctx->weather[slot], ctx->weather16[0][slot], ctx->weather16[1][slot]},
                      (cudaStream_t)stream));
+    MT_CUDA(ctx, mt::launch_cells2(ctx->weather[slot], MT_WEATHER_N, ctx->weather_c[slot], (cudaStream_t)stream));
     return MT_OK;
 }
 
@@ -471,6 +496,13 @@ MT_API mt_status mt_download_volumes_16(mt_ctx* ctx, int storage, uint16_t* base
     return MT_OK;
 }
 
+MT_API mt_status mt_set_sample_trace(mt_ctx* ctx, void* counts) {
+    if (!ctx) return MT_ERR_INVALID_ARG;
+    if (counts && !aligned(counts, 16)) return fail(ctx, MT_ERR_INVALID_ARG, "counts must be 16-byte aligned");
+    ctx->trace = static_cast<uint4*>(counts);
+    return MT_OK;
+}
+
 MT_API mt_status mt_render(mt_ctx* ctx, const mt_camera_ubo* camera, const mt_camera_ubo* camera_old,
                            const mt_time_ubo* time, const mt_params* params, const float* prev_rgba, float* cur_rgba,
                            float* godray_mask, int width, int height, uint32_t flags, void* stream) {
@@ -480,6 +512,7 @@ MT_API mt_status mt_render(mt_ctx* ctx, const mt_camera_ubo* camera, const mt_ca
                                     height, flags, &a);
     if (st != MT_OK) return st;
     if ((st = bind_device(ctx)) != MT_OK) return st;
+    a.trace = ctx->trace;
     mt::LaunchEvents ev{{ctx->ev[0], ctx->ev[1]}, {ctx->ev[2], ctx->ev[3]}, {ctx->ev[6], ctx->ev[7]}, ctx->timing};
     const mt::ForkJoin fj{ctx->aux, ctx->fork_ev, ctx->join_ev};
     MT_CUDA(ctx, mt::launch_render(a, (cudaStream_t)stream, &ev, ctx->overlap ? &fj : nullptr));
@@ -500,6 +533,7 @@ MT_API mt_status mt_render_frame(mt_ctx* ctx, const mt_camera_ubo* camera, const
                                     height, flags, &a);
     if (st != MT_OK) return st;
     if (!history_rgba || !out_rgba) return fail(ctx, MT_ERR_INVALID_ARG, "history and out must not be NULL");
+    a.trace = ctx->trace;
     if (!aligned(history_rgba, 16) || !aligned(out_rgba, 16))
         return fail(ctx, MT_ERR_INVALID_ARG, "images must be 16-byte aligned");
     if (out_rgba == cur_rgba || out_rgba == history_rgba || out_rgba == prev_rgba)

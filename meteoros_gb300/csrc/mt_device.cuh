@@ -218,69 +218,63 @@ MT_HD f4p lerp4p_fused(f4p p, f4p q, float2 t) {
 // i0 = floor(u), alpha = u - i0, REPEAT wraps the integer texel coordinate
 // (N is a power of two).  Raw texel values are interpolated x, then y, then
 // z, and the result is scaled once (1/255 for UNORM8), channels in packed
-// pairs.  The volumes are RGBA8 words, x fastest, then y, then z
-// (ImageLoadingUtility.cpp:75-139).
+// pairs.  The RGBA8 volumes are read in their filter-cell layout
+// (launch_cells3 / launch_cells2): cell (x0, y0, z0) holds the eight texels of
+// the fetch -- {(x0,y0), (x1,y0), (x0,y1), (x1,y1)} at z0, then at z1, each
+// texel an RGBA8 word of the volume (x fastest, then y, then z,
+// ImageLoadingUtility.cpp:75-139) -- so a trilinear fetch is two 16-byte
+// loads from one 32-byte sector and a bilinear fetch one 16-byte load.
 // ---------------------------------------------------------------------------
-template <int N> MT_HD f4v tex3_u8(const uint32_t* __restrict__ vol, f3 s) {
+template <int N> MT_HD f4v tex3_u8(const uint4* __restrict__ cells, f3 s) {
     constexpr unsigned M = (unsigned)N - 1u;
     const float fn = (float)N;
     float u = s.x * fn - 0.5f, v = s.y * fn - 0.5f, w = s.z * fn - 0.5f;
     float fu = floorf(u), fv = floorf(v), fw = floorf(w);
     float a = u - fu, b = v - fv, g = w - fw;
-    unsigned iu = (unsigned)f2i(fu), iv = (unsigned)f2i(fv), iw = (unsigned)f2i(fw);
-    unsigned x0 = iu & M, x1 = (iu + 1u) & M, y0 = iv & M, y1 = (iv + 1u) & M, z0 = iw & M, z1 = (iw + 1u) & M;
-    const uint32_t* p0 = vol + (size_t)z0 * (N * N);
-    const uint32_t* p1 = vol + (size_t)z1 * (N * N);
-    uint32_t t000 = __ldg(p0 + y0 * N + x0), t100 = __ldg(p0 + y0 * N + x1);
-    uint32_t t010 = __ldg(p0 + y1 * N + x0), t110 = __ldg(p0 + y1 * N + x1);
-    uint32_t t001 = __ldg(p1 + y0 * N + x0), t101 = __ldg(p1 + y0 * N + x1);
-    uint32_t t011 = __ldg(p1 + y1 * N + x0), t111 = __ldg(p1 + y1 * N + x1);
+    const unsigned x0 = (unsigned)f2i(fu) & M, y0 = (unsigned)f2i(fv) & M, z0 = (unsigned)f2i(fw) & M;
+    const uint4* c = cells + 2 * (((size_t)z0 * N + y0) * N + x0);
+    const uint4 q0 = __ldg(c), q1 = __ldg(c + 1);
     const float2 a2 = splat2(a), b2 = splat2(b), g2 = splat2(g);
-    const f4p c00 = lerp_texels(t000, t100, a2);
-    const f4p c10 = lerp_texels(t010, t110, a2);
-    const f4p c01 = lerp_texels(t001, t101, a2);
-    const f4p c11 = lerp_texels(t011, t111, a2);
+    const f4p c00 = lerp_texels(q0.x, q0.y, a2);
+    const f4p c10 = lerp_texels(q0.z, q0.w, a2);
+    const f4p c01 = lerp_texels(q1.x, q1.y, a2);
+    const f4p c11 = lerp_texels(q1.z, q1.w, a2);
     const f4p c0 = lerp4p(c00, c10, b2);
     const f4p c1 = lerp4p(c01, c11, b2);
     return scale4p(lerp4p(c0, c1, g2), 1.0f / 255.0f);
 }
 
 // tex3_u8 with fused lerps (light samples).
-template <int N> MT_HD f4v tex3_u8_fused(const uint32_t* __restrict__ vol, f3 s) {
+template <int N> MT_HD f4v tex3_u8_fused(const uint4* __restrict__ cells, f3 s) {
     constexpr unsigned M = (unsigned)N - 1u;
     const float fn = (float)N;
     float u = fmaf(s.x, fn, -0.5f), v = fmaf(s.y, fn, -0.5f), w = fmaf(s.z, fn, -0.5f);
     float fu = floorf(u), fv = floorf(v), fw = floorf(w);
     float a = u - fu, b = v - fv, g = w - fw;
-    unsigned iu = (unsigned)f2i(fu), iv = (unsigned)f2i(fv), iw = (unsigned)f2i(fw);
-    unsigned x0 = iu & M, x1 = (iu + 1u) & M, y0 = iv & M, y1 = (iv + 1u) & M, z0 = iw & M, z1 = (iw + 1u) & M;
-    const uint32_t* p0 = vol + (size_t)z0 * (N * N);
-    const uint32_t* p1 = vol + (size_t)z1 * (N * N);
-    uint32_t t000 = __ldg(p0 + y0 * N + x0), t100 = __ldg(p0 + y0 * N + x1);
-    uint32_t t010 = __ldg(p0 + y1 * N + x0), t110 = __ldg(p0 + y1 * N + x1);
-    uint32_t t001 = __ldg(p1 + y0 * N + x0), t101 = __ldg(p1 + y0 * N + x1);
-    uint32_t t011 = __ldg(p1 + y1 * N + x0), t111 = __ldg(p1 + y1 * N + x1);
+    const unsigned x0 = (unsigned)f2i(fu) & M, y0 = (unsigned)f2i(fv) & M, z0 = (unsigned)f2i(fw) & M;
+    const uint4* c = cells + 2 * (((size_t)z0 * N + y0) * N + x0);
+    const uint4 q0 = __ldg(c), q1 = __ldg(c + 1);
     const float2 a2 = splat2(a), b2 = splat2(b), g2 = splat2(g);
-    const f4p c00 = lerp_texels_fused(t000, t100, a2);
-    const f4p c10 = lerp_texels_fused(t010, t110, a2);
-    const f4p c01 = lerp_texels_fused(t001, t101, a2);
-    const f4p c11 = lerp_texels_fused(t011, t111, a2);
+    const f4p c00 = lerp_texels_fused(q0.x, q0.y, a2);
+    const f4p c10 = lerp_texels_fused(q0.z, q0.w, a2);
+    const f4p c01 = lerp_texels_fused(q1.x, q1.y, a2);
+    const f4p c11 = lerp_texels_fused(q1.z, q1.w, a2);
     const f4p c0 = lerp4p_fused(c00, c10, b2);
     const f4p c1 = lerp4p_fused(c01, c11, b2);
     return scale4p(lerp4p_fused(c0, c1, g2), 1.0f / 255.0f);
 }
 
-template <int N> MT_HD f4v tex2_u8(const uint32_t* __restrict__ img, float sx, float sy) {
+template <int N> MT_HD f4v tex2_u8(const uint4* __restrict__ cells, float sx, float sy) {
     constexpr unsigned M = (unsigned)N - 1u;
     const float fn = (float)N;
     float u = sx * fn - 0.5f, v = sy * fn - 0.5f;
     float fu = floorf(u), fv = floorf(v);
     float a = u - fu, b = v - fv;
-    unsigned iu = (unsigned)f2i(fu), iv = (unsigned)f2i(fv);
-    unsigned x0 = iu & M, x1 = (iu + 1u) & M, y0 = iv & M, y1 = (iv + 1u) & M;
+    const unsigned x0 = (unsigned)f2i(fu) & M, y0 = (unsigned)f2i(fv) & M;
+    const uint4 q = __ldg(cells + ((size_t)y0 * N + x0));
     const float2 a2 = splat2(a);
-    const f4p c0 = lerp_texels(__ldg(img + y0 * N + x0), __ldg(img + y0 * N + x1), a2);
-    const f4p c1 = lerp_texels(__ldg(img + y1 * N + x0), __ldg(img + y1 * N + x1), a2);
+    const f4p c0 = lerp_texels(q.x, q.y, a2);
+    const f4p c1 = lerp_texels(q.z, q.w, a2);
     return scale4p(lerp4p(c0, c1, splat2(b)), 1.0f / 255.0f);
 }
 

@@ -54,7 +54,8 @@ struct MarchArgs {
     mt_params params;
     // base (MT_BASE_N^3), detail (MT_DETAIL_N^3), curl (MT_CURL_N^2), weather
     // (MT_WEATHER_N^2, slot params.weather_slot) in params.storage: RGBA8
-    // words (uint32_t) or four 16-bit values (uint2)
+    // filter cells (uint4; launch_cells3 / launch_cells2) or four 16-bit
+    // values per texel (uint2)
     const void* vol[4];
     const float4* prev;
     float4* cur;
@@ -74,6 +75,10 @@ struct MarchArgs {
     const float4* history;       // mt_render_frame only: previous resolved frame
     float4* out;                 // mt_render_frame only: resolved frame
     int32_t fused_resolve;       // mt_render_frame: 1 = reprojection fused with TXAA
+    // mt_render / mt_render_frame only (NULL elsewhere): per marched pixel,
+    // the ray's executed primary samples, in-cloud samples, control-flow
+    // signature and 0 (mt_set_sample_trace)
+    uint4* trace;
     ViewConsts vc_repro;         // reprojection geometry (reprojection.comp's jitter)
     ViewConsts vc_txaa;          // TXAA geometry (cloudRayMarch.comp's jitter)
     // The raymarch's per-step jitter (cloudRayMarch.comp:629-633) for each of
@@ -195,6 +200,10 @@ cudaError_t launch_generate_detail(uint32_t seed, NoiseOut o, cudaStream_t s);
 cudaError_t launch_generate_curl(uint32_t seed, NoiseOut o, cudaStream_t s);
 cudaError_t launch_generate_weather(uint32_t seed, NoiseOut o, cudaStream_t s);
 cudaError_t launch_u8_to_16(const uint32_t* src, size_t n, uint2* h16, uint2* b16, cudaStream_t s);
+// Filter-cell copies of an RGBA8 volume (n^3 cells of 2 x uint4) or image
+// (n^2 cells of 1 x uint4), the layout the plain form's samplers read.
+cudaError_t launch_cells3(const uint32_t* vol, int n, uint4* cells, cudaStream_t s);
+cudaError_t launch_cells2(const uint32_t* img, int n, uint4* cells, cudaStream_t s);
 
 // Number of 4x4 blocks along one axis covered by the reference's raymarch
 // dispatch: ceil(floor(dim/4) / 32) groups of 32 (Renderer.cpp:713-716).

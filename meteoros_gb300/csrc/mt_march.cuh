@@ -14,7 +14,7 @@ namespace mt {
 // Storage-specific volume access.
 template <int S> struct Vol;
 template <> struct Vol<MT_STORAGE_U8> {
-    using T = uint32_t;
+    using T = uint4;  // filter cells (launch_cells3 / launch_cells2)
     template <int N> static MT_HD f4v tex3(const T* v, f3 s) { return tex3_u8<N>(v, s); }
     template <int N> static MT_HD f4v tex3_light(const T* v, f3 s) { return tex3_u8_fused<N>(v, s); }
     template <int N> static MT_HD f4v tex2(const T* v, float x, float y) { return tex2_u8<N>(v, x, y); }
@@ -152,19 +152,24 @@ MT_HD void ray_consts(const mt_params& p, const Frame& F, f3 dir, f3 startPos, f
 }
 
 struct StepOut {
-    int in_cloud;  // baseDensity > 0 (cloudRayMarch.comp:642)
-    float hfd;     // eroded density (:645)
-    float E;       // light energy (:673)
+    // bit 4: baseDensity > 0 (cloudRayMarch.comp:642).  Traced marches (TR)
+    // also carry the step's jitter index in bits 0-3 and its light samples'
+    // cbl > 0 in bits 5-10: the step's part of the control-flow signature.
+    int code;
+    float hfd;  // eroded density (:645)
+    float E;    // light energy (:673)
 };
+constexpr int kInCloud = 16;
 
 // One iteration of the march loop body (cloudRayMarch.comp:629-678) at
 // parameter t, up to the accumulation: everything that does not depend on the
 // running accumDensity / transmittance.
-template <int S>
+template <int S, bool TR>
 MT_HD StepOut eval_step(const mt_params& p, const Frame& F, const Tex<S>& tx, const mt_time_ubo& tm,
                         const float (*jitter)[3], const RayConsts& rc, float t) {
     StepOut o{0, 0.0f, 0.0f};
     const int _index = f2i(gmod((float)(tm.frame_count_mod16 + f2i(t)), 16.0f));
+    if (TR) o.code = _index & 15;
     const float* j = jitter[_index & 15];  // _index is in 0..15 for every finite t
     f3 jd = rc.dir + f3{j[0], j[1], j[2]};
     f3 pos = ld3(F.eye) + t * jd;
@@ -182,7 +187,7 @@ MT_HD StepOut eval_step(const mt_params& p, const Frame& F, const Tex<S>& tx, co
     float baseDensity = sample_low_frequency<S>(p, tx, sp, relH, wt) * 0.380f;
     if (baseDensity > 0.0f) {
         const Erosion ero = make_erosion(erosion_modifier<S>(tx, sp, relH));
-        o.in_cloud = 1;
+        o.code |= kInCloud;
         o.hfd = erode(baseDensity * 1.4f, ero);
         float dl = 0.0f;
         // The six cone-light samples (colour only: see sample_light).  Kept
@@ -198,7 +203,10 @@ MT_HD StepOut eval_step(const mt_params& p, const Frame& F, const Tex<S>& tx, co
             const f3 k = rc.koff[i];
             const f3 slp{__fadd_rn(prel.x, k.x), __fadd_rn(prel.y, k.y), __fadd_rn(prel.z, k.z)};
             const float cbl = sample_light<S>(p, tx, slp, wt);
-            if (cbl > 0.0f) dl = fmaf(fmaf(1.5f, cbl, -ero.lo), ero.r.y, dl);  // erode(1.5 * cbl)
+            if (cbl > 0.0f) {
+                dl = fmaf(fmaf(1.5f, cbl, -ero.lo), ero.r.y, dl);  // erode(1.5 * cbl)
+                if (TR) o.code |= 32 << i;
+            }
         }
         o.E = light_energy(relH, dl, baseDensity, rc.HG_light, rc.cos_q, 5.0f);
     }
@@ -212,7 +220,7 @@ MT_HD StepOut eval_step(const mt_params& p, const Frame& F, const Tex<S>& tx, co
 // colour, the early exit) is then applied in step order by an in-group scan;
 // steps past the exit are discarded.  Result, counters and control flow equal
 // the sequential loop's.
-template <int G, int S>
+template <int G, int S, bool TR>
 MT_HD f3 ray_march_group(const mt_params& p, const Frame& F, const Tex<S>& tx, const mt_time_ubo& tm,
                          const float (*jitter)[3], f3 dir, f3 startPos, float start_t, float end_t, float& accum,
                          Counts& cnt, unsigned gmask, int lane) {
@@ -240,18 +248,19 @@ MT_HD f3 ray_march_group(const mt_params& p, const Frame& F, const Tex<S>& tx, c
         for (int k = 0; k < lane; ++k) t += stepSize;
         const int valid = (t < end_t) && (s_base + lane < cap);
         StepOut o{0, 0.0f, 0.0f};
-        if (valid) o = eval_step<S>(p, F, tx, tm, jitter, rc, t);
+        if (valid) o = eval_step<S, TR>(p, F, tx, tm, jitter, rc, t);
 #pragma unroll
         for (int k = 0; k < G; ++k) {
             if (!__shfl_sync(gmask, valid, k, G)) {
                 done = true;
                 break;
             }
-            const int in_cloud = __shfl_sync(gmask, o.in_cloud, k, G);
+            const int code = __shfl_sync(gmask, o.code, k, G);
             const float hfd = __shfl_sync(gmask, o.hfd, k, G);
             const float E = __shfl_sync(gmask, o.E, k, G);
             if (lane == 0) cnt.primary++;
-            if (in_cloud) {
+            if (TR && lane == 0) cnt.sig = (cnt.sig ^ (unsigned)code) * 16777619u;  // FNV-1a step
+            if (code & kInCloud) {
                 accum = accum + hfd * 0.5f;
                 transmittance = gmix(transmittance, E, (1.0f - accum));
                 color = color + f3{transmittance, transmittance, transmittance};
@@ -273,7 +282,7 @@ MT_HD f3 ray_march_group(const mt_params& p, const Frame& F, const Tex<S>& tx, c
 
 // cloudRayMarch.comp:690-826 for one pixel, marched by a group of G lanes;
 // lane 0 stores.
-template <int G, int S>
+template <int G, int S, bool TR = false>
 MT_HD void march_pixel(const MarchArgs& a, const Frame& F, const Tex<S>& tx, int px, int py, Counts& cnt,
                        unsigned gmask, int lane) {
     const mt_params& p = a.params;
@@ -295,6 +304,7 @@ MT_HD void march_pixel(const MarchArgs& a, const Frame& F, const Tex<S>& tx, int
         if (lane == 0) {
             a.cur[o] = make_float4(bg.x, bg.y, bg.z, 1.0f);
             if (a.mask) a.mask[o] = 0.0f;
+            if (TR) a.trace[o] = make_uint4(0u, 0u, 0u, 0u);
         }
         return;
     }
@@ -304,6 +314,7 @@ MT_HD void march_pixel(const MarchArgs& a, const Frame& F, const Tex<S>& tx, int
         if (lane == 0) {
             a.cur[o] = make_float4(bg.x, bg.y, bg.z, 1.0f);
             if (a.mask) a.mask[o] = 0.0f;
+            if (TR) a.trace[o] = make_uint4(0u, 0u, 0u, 0u);
         }
         return;
     }
@@ -317,14 +328,17 @@ MT_HD void march_pixel(const MarchArgs& a, const Frame& F, const Tex<S>& tx, int
         out = ray_sphere(ray.origin, ray.direction, ec, F.Rout);
     }
     float accum = 0.0f;
-    f3 res = ray_march_group<G, S>(p, F, tx, a.time, a.jitter, ray.direction, in.point, in.t, out.t, accum, cnt, gmask,
-                                   lane);
+    if (TR) cnt.sig = 2166136261u;
+    f3 res = ray_march_group<G, S, TR>(p, F, tx, a.time, a.jitter, ray.direction, in.point, in.t, out.t, accum, cnt,
+                                       gmask, lane);
     if (lane != 0) return;
     float godAccum = accum;
     accum = accum * gsmoothstep(0.0f, 1.0f, gmin(1.0f, remap(ray.direction.y, fade, 0.2f, 0.0f, 1.0f)));
     f3 fc = mix3(bg, res, accum);
     a.cur[o] = make_float4(fc.x, fc.y, fc.z, 1.0f);
     if (a.mask) a.mask[o] = godray_value(25.0f * gmin(0.05f, 1.0f - godAccum), ray.direction.y);
+    // one ray per thread in march_kernel: lane 0's counters are this ray's
+    if (TR) a.trace[o] = make_uint4(cnt.primary, cnt.light / 6u, cnt.primary ? cnt.sig : 0u, 0u);
 }
 
 // Ray -> marched pixel.  Checkerboard: the reference's group grid covers
@@ -332,7 +346,7 @@ MT_HD void march_pixel(const MarchArgs& a, const Frame& F, const Tex<S>& tx, int
 // block's slot pixel.  Full: one ray per pixel.  G consecutive lanes (an
 // aligned segment of a warp) march one ray.  BS threads per CTA (256 by
 // default, 128 or 32 selectable), 64 registers a thread in every case.
-template <int G, int S, int BS>
+template <int G, int S, int BS, bool TR = false>
 __global__ void __launch_bounds__(BS, 1024 / BS) march_kernel(const __grid_constant__ MarchArgs a) {
     static_assert(G >= 1 && G <= 32 && (32 % G) == 0, "G must divide the warp");
     const Frame& F = a.frame;
@@ -362,7 +376,7 @@ __global__ void __launch_bounds__(BS, 1024 / BS) march_kernel(const __grid_const
         }
     }
     if (active) {
-        march_pixel<G, S>(a, F, tx, px, py, cnt, gmask, lane);
+        march_pixel<G, S, TR>(a, F, tx, px, py, cnt, gmask, lane);
         pixels = lane == 0 ? 1u : 0u;
     }
     if (a.stats) flush_counts(a.stats, cnt, pixels);
@@ -446,6 +460,15 @@ template <int S, int BS> void launch_march_bs(const MarchArgs& a, cudaStream_t s
 }
 
 template <int S> cudaError_t launch_march_storage(const MarchArgs& a, cudaStream_t s, long long rays) {
+    if (a.trace) {  // traced march (mt_set_sample_trace): 256-thread CTAs, 1 or 4 lanes
+        const int G = a.lanes == 1 ? 1 : 4;
+        const unsigned blocks = (unsigned)((rays * G + 255) / 256);
+        if (G == 1)
+            march_kernel<1, S, 256, true><<<blocks, 256, 0, s>>>(a);
+        else
+            march_kernel<4, S, 256, true><<<blocks, 256, 0, s>>>(a);
+        return cudaGetLastError();
+    }
     if (a.block == 256)
         launch_march_bs<S, 256>(a, s, rays);
     else if (a.block == 128)

@@ -263,7 +263,46 @@ __global__ void u8_to_16_kernel(const uint32_t* __restrict__ src, size_t n, uint
         (float)(v >> 24) / 255.0f);
 }
 
+// Filter-cell layout of an RGBA8 volume (what the plain form's samplers
+// read): cell (x, y, z) holds the eight texels a trilinear fetch at that cell
+// interpolates, x0 = x, x1 = (x + 1) mod N and so on (REPEAT), as two 16-byte
+// words -- {(x0,y0), (x1,y0), (x0,y1), (x1,y1)} at z0, then the same at z1 --
+// so one fetch reads one 32-byte sector.
+__global__ void cells3_kernel(const uint32_t* __restrict__ vol, int n, uint4* __restrict__ cells) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t nn = (size_t)n * n;
+    if (i >= nn * n) return;
+    const unsigned m = (unsigned)n - 1u;
+    const unsigned x = (unsigned)(i % n), y = (unsigned)((i / n) % n), z = (unsigned)(i / nn);
+    const unsigned x1 = (x + 1u) & m, y1 = (y + 1u) & m, z1 = (z + 1u) & m;
+    const uint32_t* p0 = vol + (size_t)z * nn;
+    const uint32_t* p1 = vol + (size_t)z1 * nn;
+    cells[2 * i] = make_uint4(p0[y * n + x], p0[y * n + x1], p0[y1 * n + x], p0[y1 * n + x1]);
+    cells[2 * i + 1] = make_uint4(p1[y * n + x], p1[y * n + x1], p1[y1 * n + x], p1[y1 * n + x1]);
+}
+
+// The same for an RGBA8 image (bilinear cells): {(x0,y0), (x1,y0), (x0,y1), (x1,y1)}.
+__global__ void cells2_kernel(const uint32_t* __restrict__ img, int n, uint4* __restrict__ cells) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)n * n) return;
+    const unsigned m = (unsigned)n - 1u;
+    const unsigned x = (unsigned)(i % n), y = (unsigned)(i / n);
+    const unsigned x1 = (x + 1u) & m, y1 = (y + 1u) & m;
+    cells[i] = make_uint4(img[y * n + x], img[y * n + x1], img[y1 * n + x], img[y1 * n + x1]);
+}
+
 }  // namespace
+
+cudaError_t launch_cells3(const uint32_t* vol, int n, uint4* cells, cudaStream_t s) {
+    const size_t texels = (size_t)n * n * n;
+    cells3_kernel<<<(unsigned)((texels + 255) / 256), 256, 0, s>>>(vol, n, cells);
+    return cudaGetLastError();
+}
+cudaError_t launch_cells2(const uint32_t* img, int n, uint4* cells, cudaStream_t s) {
+    const size_t texels = (size_t)n * n;
+    cells2_kernel<<<(unsigned)((texels + 255) / 256), 256, 0, s>>>(img, n, cells);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_generate_base(uint32_t seed, NoiseOut o, cudaStream_t s) {
     const unsigned n = MT_BASE_N * MT_BASE_N * MT_BASE_N;

@@ -11,7 +11,8 @@
 //   * Requests queue in arrival order.  A worker thread forms a batch from
 //     every queued request whose session has no frame in flight (a session's
 //     frame N+1 reprojects frame N), up to max_batch, and launches it with
-//     mt_render_batch.  Up to `streams` batches are in flight at once: requests
+//     mt_render_batch (a batch of one with mt_render, which skips the batch's
+//     tables).  Up to `streams` batches are in flight at once: requests
 //     that arrive while a batch runs join the next one, which overlaps on the
 //     device.  Completion is stamped by a host function queued behind the
 //     batch on its stream.
@@ -204,7 +205,9 @@ void worker_main(mt_server* s) {
         s->next_stream = (s->next_stream + 1) % std::max(1, s->cfg.streams);
         lk.unlock();
         mt_status st;
-        if (s->cfg.per_request) {
+        // A batch of one takes the direct launch: the same frame as the batched
+        // launch (equal per pixel), without building a view table and tile list.
+        if (s->cfg.per_request || views.size() == 1) {
             const mt_view& v = views[0];
             st = mt_render(s->ctx, &v.camera, &v.camera_old, &v.time, &v.params, v.prev_rgba, v.cur_rgba,
                            v.godray_mask, v.width, v.height, v.flags, stream);

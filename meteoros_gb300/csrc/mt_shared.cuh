@@ -257,6 +257,7 @@ static __device__ __noinline__ f3 atmosphere_color(const mt_params& p, f3 dir, f
 
 struct Counts {
     unsigned primary, light, rays;
+    unsigned sig;  // traced marches: control-flow signature of the ray being marched
 };
 
 // cloudRayMarch.comp:106-112 + postProcess_GodRays.frag:36-43

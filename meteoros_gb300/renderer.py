@@ -177,6 +177,12 @@ class Context:
         self._check(self.lib.mt_set_tuning(self.handle, C.byref(t)))
         return t
 
+    def set_sample_trace(self, counts=None) -> None:
+        """Per-pixel control-flow trace of later renders (mt_set_sample_trace):
+        `counts` an (H, W, 4) int32 device tensor, or None to stop."""
+        self._check(self.lib.mt_set_sample_trace(self.handle, _ptr(counts)))
+        self._trace = counts  # kept alive while the library may write it
+
     def set_timing(self, enabled: bool) -> None:
         self._check(self.lib.mt_set_timing(self.handle, 1 if enabled else 0))
 

@@ -386,7 +386,13 @@ template <class T> V3<T> atmosphere_color(const Frame<T>& F, V3<T> dir, V3<T> su
 
 struct Counters {
     uint64_t primary = 0, light = 0, rays = 0, pixels = 0;
+    // Control-flow signature of the last ray marched: an FNV-1a hash over its
+    // executed steps of (jitter index | in cloud << 4 | the six light samples'
+    // cbl > 0 bits << 5), in step order.  Two marches with equal signatures
+    // (and step counts) took the same branches at every threshold.
+    uint32_t sig = 2166136261u;
 };
+inline void sig_step(Counters& c, uint32_t code) { c.sig = (c.sig ^ code) * 16777619u; }
 
 // cloudRayMarch.comp:565-688
 template <class T> V3<T> ray_march(const Frame<T>& F, const Ray<T>& ray, V3<T> earthCenter, V3<T> startPos, T start_t,
@@ -430,10 +436,12 @@ template <class T> V3<T> ray_march(const Frame<T>& F, const Ray<T>& ray, V3<T> e
     const int cap = 2 * f2i(maxSteps) + 8;
     int it = 0;
     cnt.rays++;
+    cnt.sig = 2166136261u;
     for (T t = start_t; t < end_t; t += stepSize) {
         if (it++ >= cap) break;
         cnt.primary++;
         int _index = f2i(gmod(T(pixelID + f2i(t)), T(16)));
+        uint32_t code = (uint32_t)_index & 15u;
         V2<T> jl = jitter_offset<T>(F.tm, _index, 75, 75, false);
         V3<T> jd = ray.direction + V3<T>{jl.x, (jl.x + jl.y) * jitterfactor, jl.y};
         V3<T> pos = ray.origin + t * jd;
@@ -448,17 +456,22 @@ template <class T> V3<T> ray_march(const Frame<T>& F, const Ray<T>& ray, V3<T> e
             T hfd = erode(baseDensity * L(1.4), mod);
             accumDensity = accumDensity + hfd * L(0.5);
             T dl = T(0);
+            code |= 16u;
             for (int i = 0; i < 6; ++i) {
                 V3<T> lightPos = pos + ((stepSize * kernel[i]) * T(i));
                 V3<T> slp = relative_position(F, lightPos, earthCenter);
                 cnt.light++;
                 T cbl = sample_low_frequency(F, slp, relH, wt);
-                if (cbl > T(0)) dl = dl + erode(L(1.5) * cbl, mod);
+                if (cbl > T(0)) {
+                    dl = dl + erode(L(1.5) * cbl, mod);
+                    code |= 32u << i;
+                }
             }
             T E = light_energy(relH, dl, baseDensity, HG_light, cos_angle, stepSize, L(5.0));
             transmittance = gmix(transmittance, E, (T(1) - accumDensity));
             returnColor = returnColor + V3<T>{transmittance, transmittance, transmittance};
         }
+        sig_step(cnt, code);
         if (accumDensity >= T(p->accum_limit)) {
             accumDensity = T(1);
             break;
@@ -748,9 +761,13 @@ template <class T> int render(const orc_volumes* v, const mt_camera_ubo* cam, co
 
 // cloudRayMarch.comp:690-826 for a list of pixels (x, y pairs), each marched
 // as in a full-raymarch frame; for error statistics on a sample of a large frame.
+// counts (may be NULL): per pixel four uint32, the ray's executed primary
+// samples, its in-cloud samples (density > 0, cloudRayMarch.comp:642), its
+// control-flow signature (Counters::sig; 0 for a ray that marched no step)
+// and 0.
 template <class T> int march_pixels(const orc_volumes* v, const mt_camera_ubo* cam, const mt_time_ubo* tm,
                                     const mt_params* p, int W, int H, const int32_t* xy, long long n, T* rgba,
-                                    T* mask, int nthreads) {
+                                    T* mask, uint32_t* counts, int nthreads) {
     if (!v || !cam || !tm || !p || !xy || !rgba || W <= 0 || H <= 0 || n < 0) return 1;
     Frame<T> F = make_frame<T>(v, cam, cam, tm, p);
 #ifdef _OPENMP
@@ -768,6 +785,12 @@ template <class T> int march_pixels(const orc_volumes* v, const mt_camera_ubo* c
         rgba[4 * i + 2] = c.z;
         rgba[4 * i + 3] = c.w;
         if (mask) mask[i] = m;
+        if (counts) {
+            counts[4 * i] = (uint32_t)cnt.primary;
+            counts[4 * i + 1] = (uint32_t)(cnt.light / 6);
+            counts[4 * i + 2] = cnt.primary ? cnt.sig : 0u;
+            counts[4 * i + 3] = 0u;
+        }
     }
     return 0;
 }
@@ -838,14 +861,14 @@ __attribute__((visibility("default"))) int orc_txaa_f64(const mt_camera_ubo* cam
 __attribute__((visibility("default"))) int orc_march_pixels_f32(const orc_volumes* v, const mt_camera_ubo* cam,
                                                                 const mt_time_ubo* tm, const mt_params* p, int W,
                                                                 int H, const int32_t* xy, long long n, float* rgba,
-                                                                float* mask, int nthreads) {
-    return orc::march_pixels<float>(v, cam, tm, p, W, H, xy, n, rgba, mask, nthreads);
+                                                                float* mask, uint32_t* counts, int nthreads) {
+    return orc::march_pixels<float>(v, cam, tm, p, W, H, xy, n, rgba, mask, counts, nthreads);
 }
 __attribute__((visibility("default"))) int orc_march_pixels_f64(const orc_volumes* v, const mt_camera_ubo* cam,
                                                                 const mt_time_ubo* tm, const mt_params* p, int W,
                                                                 int H, const int32_t* xy, long long n, double* rgba,
-                                                                double* mask, int nthreads) {
-    return orc::march_pixels<double>(v, cam, tm, p, W, H, xy, n, rgba, mask, nthreads);
+                                                                double* mask, uint32_t* counts, int nthreads) {
+    return orc::march_pixels<double>(v, cam, tm, p, W, H, xy, n, rgba, mask, counts, nthreads);
 }
 
 // Single-function probes for the unit tests (float instantiation).

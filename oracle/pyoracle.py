@@ -66,7 +66,7 @@ def lib() -> C.CDLL:
         for name in ("orc_march_pixels_f32", "orc_march_pixels_f64"):
             f = getattr(L, name)
             f.restype = C.c_int
-            f.argtypes = [C.POINTER(OrcVolumes), cam, tm, par, C.c_int, C.c_int, P, C.c_longlong, P, P, C.c_int]
+            f.argtypes = [C.POINTER(OrcVolumes), cam, tm, par, C.c_int, C.c_int, P, C.c_longlong, P, P, P, C.c_int]
         L.orc_godrays_f32.restype = C.c_int
         L.orc_godrays_f32.argtypes = [cam, P, P, P, P, C.c_int, C.c_int]
         L.orc_tonemap_f32.restype = C.c_int
@@ -210,19 +210,22 @@ def render(vol: Volumes, cam, cam_old, tm, params, prev, width: int, height: int
 
 
 def march_pixels(vol: Volumes, cam, tm, params, width: int, height: int, xy: np.ndarray, dtype=np.float64,
-                 nthreads: int = 0):
-    """Full-raymarch colour and god-ray value of the listed pixels (xy: n x 2 int32)."""
+                 nthreads: int = 0, counts: bool = False):
+    """Full-raymarch colour and god-ray value of the listed pixels (xy: n x 2
+    int32); with counts=True also each ray's trace as an (n, 4) uint32 array:
+    primary samples, in-cloud samples, control-flow signature, 0."""
     xy = np.ascontiguousarray(xy, np.int32)
     n = xy.shape[0]
     rgba = np.zeros((n, 4), dtype)
     mask = np.zeros(n, dtype)
+    cnt = np.zeros((n, 4), np.uint32) if counts else None
     fn = lib().orc_march_pixels_f32 if dtype == np.float32 else lib().orc_march_pixels_f64
     v = vol.c()
     rc = fn(C.byref(v), C.byref(cam), C.byref(tm), C.byref(params), width, height, _ptr(xy), n, _ptr(rgba),
-            _ptr(mask), nthreads)
+            _ptr(mask), _ptr(cnt), nthreads)
     if rc != 0:
         raise RuntimeError(f"orc_march_pixels failed ({rc})")
-    return rgba, mask
+    return (rgba, mask, cnt) if counts else (rgba, mask)
 
 
 def volumes_16(vols: dict, storage: str) -> Volumes:

@@ -48,3 +48,17 @@ def test_reference_arm_prints_the_contract_line():
     libs = mapped[0].split()[1:]
     assert any(x.endswith("oracle/_build/liboracle.so") for x in libs), libs
     assert not any("libmeteoros_gb300" in x for x in libs), libs
+
+
+def test_gpus_n_starts_n_ranks():
+    """`bench.py --gpus 2` without a launcher runs as two ranks (torchrun on
+    127.0.0.1); rank 0 alone prints the line (the reference arm: host cores,
+    no GPU needed)."""
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--gpus", "2", "--steps", "1",
+                        "--warmup", "0"], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [x for x in r.stdout.splitlines() if x.lstrip().startswith("{")]
+    assert len(lines) == 1, r.stdout
+    d = json.loads(lines[0][lines[0].index("{"):])
+    assert d["impl"] == "reference" and d["n_gpus"] == 2
+    assert d["config"]["parallelism"] == "replicas x2"

@@ -435,3 +435,30 @@ def test_config1_chain_16_frames(ctx, oracle, vol7):
         assert m.sum() == (w * h if k == 0 else ((w - sx + 3) // 4) * ((h - sy + 3) // 4))
         assert_bits_equal(sess.mask.cpu().numpy()[m], mask[m], f"frame {k} god-ray values")
         assert (st.primary_samples, st.light_samples, st.marched_rays) == (int(cnt[0]), int(cnt[1]), int(cnt[2])), k
+
+
+@pytest.mark.parametrize("lanes", [1, 4])
+def test_per_ray_control_flow_equals_oracle(ctx, oracle, vol7, lanes):
+    """The exact FP32 form takes the same branch at every threshold as the
+    oracle, ray by ray: the traced per-pixel step counts and control-flow
+    signatures (jitter index, density > 0 and the six light samples' cbl > 0 of
+    every executed step, in order) are equal for every pixel."""
+    w, h = 160, 90
+    cam, tm, params, _ = scenes.config_view(44, w, h)
+    trace = torch.zeros((h, w, 4), dtype=torch.int32, device="cuda")
+    cur = torch.zeros((h, w, 4), dtype=torch.float32, device="cuda")
+    ctx.set_tuning(march_lanes=lanes)
+    ctx.set_sample_trace(trace)
+    try:
+        ctx.render(cam, cam, tm, params, None, cur, None, abi.MT_RENDER_FULL)
+        torch.cuda.synchronize()
+    finally:
+        ctx.set_sample_trace(None)
+        ctx.set_tuning(march_lanes=0)
+    got = trace.cpu().numpy().view(np.uint32).reshape(-1, 4)
+    ys, xs = np.mgrid[0:h, 0:w]
+    xy = np.stack([xs.ravel(), ys.ravel()], 1).astype(np.int32)
+    _, _, want = oracle.march_pixels(vol7, cam, tm, params, w, h, xy, dtype=np.float32, counts=True)
+    assert (want[:, 1] > 0).sum() > 100  # clouds in view
+    bad = ~(got == want).all(1)
+    assert not bad.any(), f"{int(bad.sum())} rays differ, first: {got[bad][:3].tolist()} vs {want[bad][:3].tolist()}"
