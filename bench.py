@@ -291,7 +291,8 @@ def bench_batched(ctx, torch, flush, reps: int = 3) -> dict:
         ms = _timed_reps(torch, flush, lambda: ctx.render_batch(views), reps)
         out[name] = {"ms": round(ms, 3), "gsamples_per_s": round(samples / (ms * 1e-3) / 1e9, 3),
                      "primary_samples": int(samples),
-                     "tile": [best.batch_tile_w, best.batch_tile_h], "lanes": best.batch_lanes}
+                     "tile": [best.batch_tile_w, best.batch_tile_h], "lanes": best.batch_lanes,
+                     "tile_rows": "top to bottom" if best.batch_order else "bottom to top"}
         if storage == abi.MT_STORAGE_U8:
             def per_view():
                 for v, (cur, mask) in zip(views, imgs):
@@ -299,7 +300,7 @@ def bench_batched(ctx, torch, flush, reps: int = 3) -> dict:
             pms = _timed_reps(torch, flush, per_view, reps)
             out["per_view_u8_fp32"] = {"ms": round(pms, 3),
                                        "gsamples_per_s": round(samples / (pms * 1e-3) / 1e9, 3)}
-    ctx.set_tuning(batch_tile=(16, 8), batch_lanes=1)
+    ctx.set_tuning(batch_tile=(16, 8), batch_lanes=1, batch_order=0)
     return out
 
 

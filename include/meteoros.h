@@ -168,10 +168,12 @@ typedef struct mt_tuning {
                                * runs on a second stream beside the raymarch (default; the call
                                * still completes in `stream` order); 1 = before it on `stream` */
     int32_t march_block;   /* mt_render: raymarch CTA size, 32, 128 or 256 threads; 0 = default (256) */
-    int32_t march_order;   /* mt_render / mt_render_batch: 0 = ray rows dispatched bottom to top
-                            * (default: the rows below the horizon, which do not march, first,
-                            * then the marching rows from the horizon up); 1 = top to bottom */
-    int32_t _reserved[3];
+    int32_t march_order;   /* mt_render: 0 = ray rows dispatched bottom to top (default: the rows
+                            * below the horizon, which do not march, first, then the marching rows
+                            * from the horizon up); 1 = top to bottom */
+    int32_t batch_order;   /* mt_render_batch: the order each view's tile rows are handed out in,
+                            * 0 = bottom to top (default), 1 = top to bottom */
+    int32_t _reserved[2];
 } mt_tuning;
 
 /* One view of a batched render (config 3). */
@@ -318,9 +320,13 @@ MT_API mt_status mt_render_batch(mt_ctx* ctx, const mt_view* views, int n_views,
  * 1 or 4 lanes per ray and 256-thread CTAs; batched renders never write it. */
 MT_API mt_status mt_set_sample_trace(mt_ctx* ctx, void* counts);
 
-/* Times mt_render_batch on these views for every tile shape in
- * {8x8, 16x8, 16x16, 32x8} and lanes in {1, 4}, keeps the fastest in the
- * context's tuning and returns it (the views are rendered several times). */
+/* Times mt_render_batch on these views over the tile shapes {8x8, 16x8,
+ * 16x16, 32x8} and the step schedule -- the lanes that march one ray (1, 4
+ * or 8: a ray's primary steps evaluated one at a time, or 4 / 8 at once with
+ * the in-order scan) and the order the tile rows are handed out (bottom to
+ * top or top to bottom) -- keeps the fastest in the context's tuning
+ * (batch_tile_w/h, batch_lanes, batch_order) and returns it.  Each point is
+ * timed twice and its faster run kept; the views are rendered 49 times. */
 MT_API mt_status mt_autotune_batch(mt_ctx* ctx, const mt_view* views, int n_views, void* stream,
                                    mt_tuning* best);
 

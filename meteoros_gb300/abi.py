@@ -117,7 +117,7 @@ class Tuning(C.Structure):
     _fields_ = [("march_lanes", C.c_int32), ("fused_resolve", C.c_int32), ("batch_tile_w", C.c_int32),
                 ("batch_tile_h", C.c_int32), ("batch_lanes", C.c_int32), ("batch_direct", C.c_int32),
                 ("reproject_serial", C.c_int32), ("march_block", C.c_int32),
-                ("march_order", C.c_int32), ("_reserved", C.c_int32 * 3)]
+                ("march_order", C.c_int32), ("batch_order", C.c_int32), ("_reserved", C.c_int32 * 2)]
 
 
 class KernelTimes(C.Structure):

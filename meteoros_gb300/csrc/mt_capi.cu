@@ -32,11 +32,14 @@ struct mt_ctx {
     uint2* curl16[2] = {nullptr, nullptr};
     std::vector<uint32_t*> weather;           // MT_MAX_WEATHER_SLOTS entries, allocated on demand
     std::vector<uint2*> weather16[2];
-    // filter-cell copies of the RGBA8 volumes (the plain form's samplers read these)
-    uint4* base_c = nullptr;                  // MT_BASE_N^3 x 2
-    uint4* detail_c = nullptr;                // MT_DETAIL_N^3 x 2
-    uint4* curl_c = nullptr;                  // MT_CURL_N^2
-    std::vector<uint4*> weather_c;            // MT_WEATHER_N^2 per slot
+    // plane-quad / bilinear-cell copies of the RGBA8 volumes (the plain form's samplers read these)
+    uint4* base_c = nullptr;                  // MT_BASE_N^3 plane quads
+    uint4* detail_c = nullptr;                // MT_DETAIL_N^3 plane quads
+    uint4* curl_c = nullptr;                  // MT_CURL_N^2 cells
+    std::vector<uint4*> weather_c;            // MT_WEATHER_N^2 cells per slot
+    // plane-quad copies of the 16-bit volumes (the precision form's 3D samplers read these)
+    uint4* base16q[2] = {nullptr, nullptr};   // MT_BASE_N^3 x 2
+    uint4* detail16q[2] = {nullptr, nullptr}; // MT_DETAIL_N^3 x 2
     bool have_base = false, have_detail = false, have_curl = false;
     unsigned long long* stats = nullptr;      // 4 counters
     bool timing = false;
@@ -45,6 +48,7 @@ struct mt_ctx {
     int march_lanes = 0;                      // step-parallel lanes per ray (mt_set_tuning); 0 = auto
     int march_block = 256;                    // march_kernel CTA size (mt_set_tuning)
     int march_order = 0;                      // ray rows: 0 bottom to top, 1 top to bottom
+    int batch_order = 0;                      // mt_render_batch tile rows: 0 bottom to top, 1 top to bottom
     int fused_resolve = 0;                    // mt_render_frame: reprojection fused with TXAA
     // mt_render_batch
     int batch_tile_w = 16, batch_tile_h = 8, batch_lanes = 1;
@@ -154,18 +158,32 @@ mt_status ensure_weather(mt_ctx* ctx, int slot) {
     return alloc(ctx, &ctx->weather16[1][slot], kWeatherTexels);
 }
 
+// The plane-quad copies of a volume's two 16-bit versions, after they change.
+cudaError_t refresh_quads(mt_ctx* ctx, int volume, cudaStream_t s) {
+    const bool base = volume == MT_VOLUME_BASE;
+    for (int k = 0; k < 2; ++k) {
+        const cudaError_t e = mt::launch_quads16(base ? ctx->base16[k] : ctx->detail16[k],
+                                                 base ? MT_BASE_N : MT_DETAIL_N,
+                                                 base ? ctx->base16q[k] : ctx->detail16q[k], s);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 mt_status ensure_volumes(mt_ctx* ctx) {
     mt_status st;
     if ((st = alloc(ctx, &ctx->base, kBaseTexels)) != MT_OK) return st;
     if ((st = alloc(ctx, &ctx->detail, kDetailTexels)) != MT_OK) return st;
     if ((st = alloc(ctx, &ctx->curl, kCurlTexels)) != MT_OK) return st;
-    if ((st = alloc(ctx, &ctx->base_c, 2 * kBaseTexels)) != MT_OK) return st;
-    if ((st = alloc(ctx, &ctx->detail_c, 2 * kDetailTexels)) != MT_OK) return st;
+    if ((st = alloc(ctx, &ctx->base_c, kBaseTexels)) != MT_OK) return st;
+    if ((st = alloc(ctx, &ctx->detail_c, kDetailTexels)) != MT_OK) return st;
     if ((st = alloc(ctx, &ctx->curl_c, kCurlTexels)) != MT_OK) return st;
     for (int k = 0; k < 2; ++k) {
         if ((st = alloc(ctx, &ctx->base16[k], kBaseTexels)) != MT_OK) return st;
         if ((st = alloc(ctx, &ctx->detail16[k], kDetailTexels)) != MT_OK) return st;
         if ((st = alloc(ctx, &ctx->curl16[k], kCurlTexels)) != MT_OK) return st;
+        if ((st = alloc(ctx, &ctx->base16q[k], 2 * kBaseTexels)) != MT_OK) return st;
+        if ((st = alloc(ctx, &ctx->detail16q[k], 2 * kDetailTexels)) != MT_OK) return st;
     }
     return MT_OK;
 }
@@ -204,8 +222,8 @@ mt_status build_march_args(mt_ctx* ctx, const mt_camera_ubo* cam, const mt_camer
         a->vol[2] = ctx->curl_c;
         a->vol[3] = weather8;  // never read when coverage_mode == 0
     } else {
-        a->vol[0] = ctx->base16[k];
-        a->vol[1] = ctx->detail16[k];
+        a->vol[0] = ctx->base16q[k];
+        a->vol[1] = ctx->detail16q[k];
         a->vol[2] = ctx->curl16[k];
         a->vol[3] = weather16;
     }
@@ -288,6 +306,8 @@ MT_API void mt_destroy(mt_ctx* ctx) {
     for (uint4* w : ctx->weather_c) cudaFree(w);
     for (int k = 0; k < 2; ++k) {
         cudaFree(ctx->base16[k]);
+        cudaFree(ctx->base16q[k]);
+        cudaFree(ctx->detail16q[k]);
         cudaFree(ctx->detail16[k]);
         cudaFree(ctx->curl16[k]);
         for (uint2* w : ctx->weather16[k]) cudaFree(w);
@@ -327,13 +347,15 @@ MT_API mt_status mt_upload_volumes(mt_ctx* ctx, const uint8_t* base, const uint8
     if (base) {
         MT_CUDA(ctx, cudaMemcpy(ctx->base, base, kBaseTexels * 4, cudaMemcpyHostToDevice));
         MT_CUDA(ctx, mt::launch_u8_to_16(ctx->base, kBaseTexels, ctx->base16[0], ctx->base16[1], 0));
-        MT_CUDA(ctx, mt::launch_cells3(ctx->base, MT_BASE_N, ctx->base_c, 0));
+        MT_CUDA(ctx, mt::launch_quads3(ctx->base, MT_BASE_N, ctx->base_c, 0));
+        MT_CUDA(ctx, refresh_quads(ctx, MT_VOLUME_BASE, 0));
         ctx->have_base = true;
     }
     if (detail) {
         MT_CUDA(ctx, cudaMemcpy(ctx->detail, detail, kDetailTexels * 4, cudaMemcpyHostToDevice));
         MT_CUDA(ctx, mt::launch_u8_to_16(ctx->detail, kDetailTexels, ctx->detail16[0], ctx->detail16[1], 0));
-        MT_CUDA(ctx, mt::launch_cells3(ctx->detail, MT_DETAIL_N, ctx->detail_c, 0));
+        MT_CUDA(ctx, mt::launch_quads3(ctx->detail, MT_DETAIL_N, ctx->detail_c, 0));
+        MT_CUDA(ctx, refresh_quads(ctx, MT_VOLUME_DETAIL, 0));
         ctx->have_detail = true;
     }
     if (curl) {
@@ -396,7 +418,8 @@ MT_API mt_status mt_decode_tga_volume(mt_ctx* ctx, int volume, const uint8_t* co
     if (e == cudaSuccess)
         e = mt::launch_u8_to_16(vol, texels, volume == MT_VOLUME_BASE ? ctx->base16[0] : ctx->detail16[0],
                                 volume == MT_VOLUME_BASE ? ctx->base16[1] : ctx->detail16[1], s);
-    if (e == cudaSuccess) e = mt::launch_cells3(vol, n, volume == MT_VOLUME_BASE ? ctx->base_c : ctx->detail_c, s);
+    if (e == cudaSuccess) e = mt::launch_quads3(vol, n, volume == MT_VOLUME_BASE ? ctx->base_c : ctx->detail_c, s);
+    if (e == cudaSuccess) e = refresh_quads(ctx, volume, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     cudaFree(d_blob);
     cudaFree(d_table);
@@ -435,9 +458,11 @@ MT_API mt_status mt_generate_volumes(mt_ctx* ctx, uint64_t seed, void* stream) {
     MT_CUDA(ctx, mt::launch_generate_base(s32, mt::NoiseOut{ctx->base, ctx->base16[0], ctx->base16[1]}, s));
     MT_CUDA(ctx, mt::launch_generate_detail(s32, mt::NoiseOut{ctx->detail, ctx->detail16[0], ctx->detail16[1]}, s));
     MT_CUDA(ctx, mt::launch_generate_curl(s32, mt::NoiseOut{ctx->curl, ctx->curl16[0], ctx->curl16[1]}, s));
-    MT_CUDA(ctx, mt::launch_cells3(ctx->base, MT_BASE_N, ctx->base_c, s));
-    MT_CUDA(ctx, mt::launch_cells3(ctx->detail, MT_DETAIL_N, ctx->detail_c, s));
+    MT_CUDA(ctx, mt::launch_quads3(ctx->base, MT_BASE_N, ctx->base_c, s));
+    MT_CUDA(ctx, mt::launch_quads3(ctx->detail, MT_DETAIL_N, ctx->detail_c, s));
     MT_CUDA(ctx, mt::launch_cells2(ctx->curl, MT_CURL_N, ctx->curl_c, s));
+    MT_CUDA(ctx, refresh_quads(ctx, MT_VOLUME_BASE, s));
+    MT_CUDA(ctx, refresh_quads(ctx, MT_VOLUME_DETAIL, s));
     ctx->have_base = ctx->have_detail = ctx->have_curl = true;
     return mt_generate_weather(ctx, 0, seed, stream);
 }
@@ -718,6 +743,7 @@ MT_API mt_status mt_render_batch(mt_ctx* ctx, const mt_view* views, int n_views,
         if (v.params.storage != views[0].params.storage)
             return fail(ctx, MT_ERR_INVALID_ARG, "view %d: all views of a batch must share one storage", i);
         count = count || (v.flags & MT_RENDER_COUNT);
+        args[(size_t)i].bottom_up = ctx->batch_order == 0 ? 1 : 0;  // the order tile rows are handed out
     }
     // Tiles, most expensive views first (rays x steps), so the persistent
     // launch does not end on one large view.
@@ -843,37 +869,45 @@ MT_API mt_status mt_autotune_batch(mt_ctx* ctx, const mt_view* views, int n_view
     mt_status st;
     if ((st = bind_device(ctx)) != MT_OK) return st;
     const int shapes[4][2] = {{8, 8}, {16, 8}, {16, 16}, {32, 8}};
-    const int lane_choices[2] = {1, 4};
+    const int lane_choices[3] = {1, 4, 8};
     cudaEvent_t t0, t1;
     MT_CUDA(ctx, cudaEventCreate(&t0));
     MT_CUDA(ctx, cudaEventCreate(&t1));
     float best_ms = -1.0f;
-    int bw = ctx->batch_tile_w, bh = ctx->batch_tile_h, bl = ctx->batch_lanes;
+    int bw = ctx->batch_tile_w, bh = ctx->batch_tile_h, bl = ctx->batch_lanes, bo = ctx->batch_order;
     st = mt_render_batch(ctx, views, n_views, stream);  // warm-up
-    for (int li = 0; st == MT_OK && li < 2; ++li)
-        for (int si = 0; st == MT_OK && si < 4; ++si) {
-            ctx->batch_tile_w = shapes[si][0];
-            ctx->batch_tile_h = shapes[si][1];
-            ctx->batch_lanes = lane_choices[li];
-            cudaEventRecord(t0, (cudaStream_t)stream);
-            st = mt_render_batch(ctx, views, n_views, stream);
-            cudaEventRecord(t1, (cudaStream_t)stream);
-            if (st != MT_OK) break;
-            float ms = 0.0f;
-            cudaEventSynchronize(t1);
-            cudaEventElapsedTime(&ms, t0, t1);
-            if (best_ms < 0.0f || ms < best_ms) {
-                best_ms = ms;
-                bw = shapes[si][0];
-                bh = shapes[si][1];
-                bl = lane_choices[li];
+    for (int oi = 0; st == MT_OK && oi < 2; ++oi)
+        for (int li = 0; st == MT_OK && li < 3; ++li)
+            for (int si = 0; st == MT_OK && si < 4; ++si) {
+                ctx->batch_tile_w = shapes[si][0];
+                ctx->batch_tile_h = shapes[si][1];
+                ctx->batch_lanes = lane_choices[li];
+                ctx->batch_order = oi;
+                float ms = -1.0f;
+                for (int rep = 0; st == MT_OK && rep < 2; ++rep) {  // the faster of two runs
+                    cudaEventRecord(t0, (cudaStream_t)stream);
+                    st = mt_render_batch(ctx, views, n_views, stream);
+                    cudaEventRecord(t1, (cudaStream_t)stream);
+                    if (st != MT_OK) break;
+                    float m = 0.0f;
+                    cudaEventSynchronize(t1);
+                    cudaEventElapsedTime(&m, t0, t1);
+                    if (ms < 0.0f || m < ms) ms = m;
+                }
+                if (st == MT_OK && (best_ms < 0.0f || ms < best_ms)) {
+                    best_ms = ms;
+                    bw = shapes[si][0];
+                    bh = shapes[si][1];
+                    bl = lane_choices[li];
+                    bo = oi;
+                }
             }
-        }
     cudaEventDestroy(t0);
     cudaEventDestroy(t1);
     ctx->batch_tile_w = bw;
     ctx->batch_tile_h = bh;
     ctx->batch_lanes = bl;
+    ctx->batch_order = bo;
     if (st != MT_OK) return st;
     return mt_get_tuning(ctx, best);
 }
@@ -913,6 +947,7 @@ MT_API mt_status mt_set_tuning(mt_ctx* ctx, const mt_tuning* t) {
     if (t->march_block != 0 && t->march_block != 32 && t->march_block != 128 && t->march_block != 256)
         return fail(ctx, MT_ERR_INVALID_ARG, "march_block must be 0 (default 256), 32, 128 or 256");
     if (t->march_order != 0 && t->march_order != 1) return fail(ctx, MT_ERR_INVALID_ARG, "march_order must be 0 or 1");
+    if (t->batch_order != 0 && t->batch_order != 1) return fail(ctx, MT_ERR_INVALID_ARG, "batch_order must be 0 or 1");
     ctx->march_lanes = t->march_lanes;
     ctx->fused_resolve = t->fused_resolve;
     ctx->batch_tile_w = t->batch_tile_w;
@@ -922,6 +957,7 @@ MT_API mt_status mt_set_tuning(mt_ctx* ctx, const mt_tuning* t) {
     ctx->overlap = t->reproject_serial ? 0 : 1;
     ctx->march_block = t->march_block == 0 ? 256 : t->march_block;
     ctx->march_order = t->march_order;
+    ctx->batch_order = t->batch_order;
     return MT_OK;
 }
 
@@ -938,6 +974,7 @@ MT_API mt_status mt_get_tuning(mt_ctx* ctx, mt_tuning* t) {
     t->reproject_serial = ctx->overlap ? 0 : 1;
     t->march_block = ctx->march_block;
     t->march_order = ctx->march_order;
+    t->batch_order = ctx->batch_order;
     return MT_OK;
 }
 
@@ -1112,7 +1149,7 @@ MT_API mt_status mt_render_batch_noalloc(mt_ctx* ctx, const mt_view* views, int 
             return fail(ctx, MT_ERR_INVALID_ARG, "view %d: all views of a batch must share one storage", i);
         count = count || (v.flags & MT_RENDER_COUNT);
         ray_grid(a, &nx[i], &ny[i]);
-        bu[i] = a.bottom_up;
+        bu[i] = ctx->batch_order == 0 ? 1 : 0;  // the order tile rows are handed out
         // most expensive views first, stable (mt_render_batch's order)
         cost[i] = (double)nx[i] * ny[i] * std::max(a.params.steps_min, a.params.steps_max);
         int j = i;

@@ -218,22 +218,22 @@ MT_HD f4p lerp4p_fused(f4p p, f4p q, float2 t) {
 // i0 = floor(u), alpha = u - i0, REPEAT wraps the integer texel coordinate
 // (N is a power of two).  Raw texel values are interpolated x, then y, then
 // z, and the result is scaled once (1/255 for UNORM8), channels in packed
-// pairs.  The RGBA8 volumes are read in their filter-cell layout
-// (launch_cells3 / launch_cells2): cell (x0, y0, z0) holds the eight texels of
-// the fetch -- {(x0,y0), (x1,y0), (x0,y1), (x1,y1)} at z0, then at z1, each
-// texel an RGBA8 word of the volume (x fastest, then y, then z,
-// ImageLoadingUtility.cpp:75-139) -- so a trilinear fetch is two 16-byte
-// loads from one 32-byte sector and a bilinear fetch one 16-byte load.
+// pairs.  The RGBA8 volumes are read in their plane-quad layout
+// (launch_quads3): entry (x0, y0, z) holds the four texels {(x0,y0), (x1,y0),
+// (x0,y1), (x1,y1)} of plane z, each an RGBA8 word of the volume (x fastest,
+// then y, then z, ImageLoadingUtility.cpp:75-139), so a trilinear fetch is two
+// 16-byte loads (planes z0 and z1); the images are read in bilinear cells
+// (launch_cells2), one 16-byte load per fetch.
 // ---------------------------------------------------------------------------
-template <int N> MT_HD f4v tex3_u8(const uint4* __restrict__ cells, f3 s) {
+template <int N> MT_HD f4v tex3_u8(const uint4* __restrict__ quads, f3 s) {
     constexpr unsigned M = (unsigned)N - 1u;
     const float fn = (float)N;
     float u = s.x * fn - 0.5f, v = s.y * fn - 0.5f, w = s.z * fn - 0.5f;
     float fu = floorf(u), fv = floorf(v), fw = floorf(w);
     float a = u - fu, b = v - fv, g = w - fw;
     const unsigned x0 = (unsigned)f2i(fu) & M, y0 = (unsigned)f2i(fv) & M, z0 = (unsigned)f2i(fw) & M;
-    const uint4* c = cells + 2 * (((size_t)z0 * N + y0) * N + x0);
-    const uint4 q0 = __ldg(c), q1 = __ldg(c + 1);
+    const uint4 q0 = __ldg(quads + (((size_t)z0 * N + y0) * N + x0));
+    const uint4 q1 = __ldg(quads + (((size_t)((z0 + 1u) & M) * N + y0) * N + x0));
     const float2 a2 = splat2(a), b2 = splat2(b), g2 = splat2(g);
     const f4p c00 = lerp_texels(q0.x, q0.y, a2);
     const f4p c10 = lerp_texels(q0.z, q0.w, a2);
@@ -245,15 +245,15 @@ template <int N> MT_HD f4v tex3_u8(const uint4* __restrict__ cells, f3 s) {
 }
 
 // tex3_u8 with fused lerps (light samples).
-template <int N> MT_HD f4v tex3_u8_fused(const uint4* __restrict__ cells, f3 s) {
+template <int N> MT_HD f4v tex3_u8_fused(const uint4* __restrict__ quads, f3 s) {
     constexpr unsigned M = (unsigned)N - 1u;
     const float fn = (float)N;
     float u = fmaf(s.x, fn, -0.5f), v = fmaf(s.y, fn, -0.5f), w = fmaf(s.z, fn, -0.5f);
     float fu = floorf(u), fv = floorf(v), fw = floorf(w);
     float a = u - fu, b = v - fv, g = w - fw;
     const unsigned x0 = (unsigned)f2i(fu) & M, y0 = (unsigned)f2i(fv) & M, z0 = (unsigned)f2i(fw) & M;
-    const uint4* c = cells + 2 * (((size_t)z0 * N + y0) * N + x0);
-    const uint4 q0 = __ldg(c), q1 = __ldg(c + 1);
+    const uint4 q0 = __ldg(quads + (((size_t)z0 * N + y0) * N + x0));
+    const uint4 q1 = __ldg(quads + (((size_t)((z0 + 1u) & M) * N + y0) * N + x0));
     const float2 a2 = splat2(a), b2 = splat2(b), g2 = splat2(g);
     const f4p c00 = lerp_texels_fused(q0.x, q0.y, a2);
     const f4p c10 = lerp_texels_fused(q0.z, q0.w, a2);
@@ -312,34 +312,69 @@ template <class P> MT_HD f4v pair_to_f4(PairTexel<P> c) {
     return f4v{rg.x, rg.y, ba.x, ba.y};
 }
 
-template <int N, class P> MT_HD f4v tex3_p16(const uint2* __restrict__ vol, f3 s) {
+// The 16-bit volumes in their plane-quad layout (launch_quads16): entry
+// (x0, y0, z) holds {(x0,y0), (x1,y0)} and {(x0,y1), (x1,y1)} of plane z, so a
+// trilinear fetch is two 32-byte entries (planes z0 and z1), four 16-byte
+// loads; the lerps run in the pair type (weights rounded to it).
+template <class P> MT_HD PairTexel<P> pair_lo(uint4 q) {
+    return PairTexel<P>{Pair<P>::from_bits(q.x), Pair<P>::from_bits(q.y)};
+}
+template <class P> MT_HD PairTexel<P> pair_hi(uint4 q) {
+    return PairTexel<P>{Pair<P>::from_bits(q.z), Pair<P>::from_bits(q.w)};
+}
+template <int N, class P> MT_HD f4v tex3_p16q(const uint4* __restrict__ quads, f3 s) {
     constexpr unsigned M = (unsigned)N - 1u;
     const float fn = (float)N;
     float u = s.x * fn - 0.5f, v = s.y * fn - 0.5f, w = s.z * fn - 0.5f;
     float fu = floorf(u), fv = floorf(v), fw = floorf(w);
     const P a = Pair<P>::splat(u - fu), b = Pair<P>::splat(v - fv), g = Pair<P>::splat(w - fw);
-    unsigned iu = (unsigned)f2i(fu), iv = (unsigned)f2i(fv), iw = (unsigned)f2i(fw);
-    unsigned x0 = iu & M, x1 = (iu + 1u) & M, y0 = iv & M, y1 = (iv + 1u) & M, z0 = iw & M, z1 = (iw + 1u) & M;
-    const uint2* p0 = vol + (size_t)z0 * (N * N);
-    const uint2* p1 = vol + (size_t)z1 * (N * N);
-    PairTexel<P> c00 = lerp_pair(ld_pair<P>(p0 + y0 * N + x0), ld_pair<P>(p0 + y0 * N + x1), a);
-    PairTexel<P> c10 = lerp_pair(ld_pair<P>(p0 + y1 * N + x0), ld_pair<P>(p0 + y1 * N + x1), a);
-    PairTexel<P> c01 = lerp_pair(ld_pair<P>(p1 + y0 * N + x0), ld_pair<P>(p1 + y0 * N + x1), a);
-    PairTexel<P> c11 = lerp_pair(ld_pair<P>(p1 + y1 * N + x0), ld_pair<P>(p1 + y1 * N + x1), a);
+    const unsigned x0 = (unsigned)f2i(fu) & M, y0 = (unsigned)f2i(fv) & M, z0 = (unsigned)f2i(fw) & M;
+    const unsigned z1 = (z0 + 1u) & M;
+    const uint4* q0 = quads + 2 * (((size_t)z0 * N + y0) * N + x0);
+    const uint4* q1 = quads + 2 * (((size_t)z1 * N + y0) * N + x0);
+    const uint4 e00 = __ldg(q0), e01 = __ldg(q0 + 1), e10 = __ldg(q1), e11 = __ldg(q1 + 1);
+    PairTexel<P> c00 = lerp_pair(pair_lo<P>(e00), pair_hi<P>(e00), a);
+    PairTexel<P> c10 = lerp_pair(pair_lo<P>(e01), pair_hi<P>(e01), a);
+    PairTexel<P> c01 = lerp_pair(pair_lo<P>(e10), pair_hi<P>(e10), a);
+    PairTexel<P> c11 = lerp_pair(pair_lo<P>(e11), pair_hi<P>(e11), a);
     return pair_to_f4(lerp_pair(lerp_pair(c00, c10, b), lerp_pair(c01, c11, b), g));
 }
 
-template <int N, class P> MT_HD f4v tex2_p16(const uint2* __restrict__ img, float sx, float sy) {
+// The same fetch with FP32 weights and FP32 lerps of the 16-bit texel values
+// (each pair widened to float2, then the packed FP32 pairs of the RGBA8 path).
+template <class P> MT_HD f4p widen(uint32_t rg, uint32_t ba) {
+    return f4p{Pair<P>::to_float2(Pair<P>::from_bits(rg)), Pair<P>::to_float2(Pair<P>::from_bits(ba))};
+}
+template <int N, class P> MT_HD f4v tex3_p16q_f32(const uint4* __restrict__ quads, f3 s) {
+    constexpr unsigned M = (unsigned)N - 1u;
+    const float fn = (float)N;
+    float u = s.x * fn - 0.5f, v = s.y * fn - 0.5f, w = s.z * fn - 0.5f;
+    float fu = floorf(u), fv = floorf(v), fw = floorf(w);
+    const float2 a2 = splat2(u - fu), b2 = splat2(v - fv), g2 = splat2(w - fw);
+    const unsigned x0 = (unsigned)f2i(fu) & M, y0 = (unsigned)f2i(fv) & M, z0 = (unsigned)f2i(fw) & M;
+    const unsigned z1 = (z0 + 1u) & M;
+    const uint4* q0 = quads + 2 * (((size_t)z0 * N + y0) * N + x0);
+    const uint4* q1 = quads + 2 * (((size_t)z1 * N + y0) * N + x0);
+    const uint4 e00 = __ldg(q0), e01 = __ldg(q0 + 1), e10 = __ldg(q1), e11 = __ldg(q1 + 1);
+    const f4p c00 = lerp4p_fused(widen<P>(e00.x, e00.y), widen<P>(e00.z, e00.w), a2);
+    const f4p c10 = lerp4p_fused(widen<P>(e01.x, e01.y), widen<P>(e01.z, e01.w), a2);
+    const f4p c01 = lerp4p_fused(widen<P>(e10.x, e10.y), widen<P>(e10.z, e10.w), a2);
+    const f4p c11 = lerp4p_fused(widen<P>(e11.x, e11.y), widen<P>(e11.z, e11.w), a2);
+    return unpack4(lerp4p_fused(lerp4p_fused(c00, c10, b2), lerp4p_fused(c01, c11, b2), g2));
+}
+template <int N, class P> MT_HD f4v tex2_p16_f32(const uint2* __restrict__ img, float sx, float sy) {
     constexpr unsigned M = (unsigned)N - 1u;
     const float fn = (float)N;
     float u = sx * fn - 0.5f, v = sy * fn - 0.5f;
     float fu = floorf(u), fv = floorf(v);
-    const P a = Pair<P>::splat(u - fu), b = Pair<P>::splat(v - fv);
+    const float2 a2 = splat2(u - fu), b2 = splat2(v - fv);
     unsigned iu = (unsigned)f2i(fu), iv = (unsigned)f2i(fv);
     unsigned x0 = iu & M, x1 = (iu + 1u) & M, y0 = iv & M, y1 = (iv + 1u) & M;
-    PairTexel<P> c0 = lerp_pair(ld_pair<P>(img + y0 * N + x0), ld_pair<P>(img + y0 * N + x1), a);
-    PairTexel<P> c1 = lerp_pair(ld_pair<P>(img + y1 * N + x0), ld_pair<P>(img + y1 * N + x1), a);
-    return pair_to_f4(lerp_pair(c0, c1, b));
+    const uint2 t00 = __ldg(img + y0 * N + x0), t10 = __ldg(img + y0 * N + x1);
+    const uint2 t01 = __ldg(img + y1 * N + x0), t11 = __ldg(img + y1 * N + x1);
+    const f4p c0 = lerp4p_fused(widen<P>(t00.x, t00.y), widen<P>(t10.x, t10.y), a2);
+    const f4p c1 = lerp4p_fused(widen<P>(t01.x, t01.y), widen<P>(t11.x, t11.y), a2);
+    return unpack4(lerp4p_fused(c0, c1, b2));
 }
 
 // Bilinear sample of an RGBA32F frame with CLAMP_TO_BORDER, opaque black

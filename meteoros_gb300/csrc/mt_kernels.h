@@ -53,9 +53,11 @@ struct MarchArgs {
     mt_time_ubo time;
     mt_params params;
     // base (MT_BASE_N^3), detail (MT_DETAIL_N^3), curl (MT_CURL_N^2), weather
-    // (MT_WEATHER_N^2, slot params.weather_slot) in params.storage: RGBA8
-    // filter cells (uint4; launch_cells3 / launch_cells2) or four 16-bit
-    // values per texel (uint2)
+    // (MT_WEATHER_N^2, slot params.weather_slot) in params.storage: for RGBA8
+    // plane quads of the volumes and bilinear cells of the images (uint4;
+    // launch_quads3 / launch_cells2), for the 16-bit storages plane quads of
+    // the volumes (2 x uint4; launch_quads16) and four 16-bit values per texel
+    // (uint2) of the images
     const void* vol[4];
     const float4* prev;
     float4* cur;
@@ -200,10 +202,13 @@ cudaError_t launch_generate_detail(uint32_t seed, NoiseOut o, cudaStream_t s);
 cudaError_t launch_generate_curl(uint32_t seed, NoiseOut o, cudaStream_t s);
 cudaError_t launch_generate_weather(uint32_t seed, NoiseOut o, cudaStream_t s);
 cudaError_t launch_u8_to_16(const uint32_t* src, size_t n, uint2* h16, uint2* b16, cudaStream_t s);
-// Filter-cell copies of an RGBA8 volume (n^3 cells of 2 x uint4) or image
-// (n^2 cells of 1 x uint4), the layout the plain form's samplers read.
-cudaError_t launch_cells3(const uint32_t* vol, int n, uint4* cells, cudaStream_t s);
+// The layouts the plain form's samplers read: plane quads of an RGBA8 volume
+// (n^3 x uint4) and bilinear cells of an RGBA8 image (n^2 x uint4).
+cudaError_t launch_quads3(const uint32_t* vol, int n, uint4* quads, cudaStream_t s);
 cudaError_t launch_cells2(const uint32_t* img, int n, uint4* cells, cudaStream_t s);
+// Plane-quad copies of a 16-bit volume (n^3 entries of 2 x uint4), the layout
+// the precision form's 3D samplers read.
+cudaError_t launch_quads16(const uint2* vol, int n, uint4* quads, cudaStream_t s);
 
 // Number of 4x4 blocks along one axis covered by the reference's raymarch
 // dispatch: ceil(floor(dim/4) / 32) groups of 32 (Renderer.cpp:713-716).

@@ -1,8 +1,9 @@
 // The raymarch kernel (cloudRayMarch.comp:565-826), templated on the lanes
 // per ray and on the storage of the noise volumes:
 //   MT_STORAGE_U8    RGBA8 volumes, exact FP32 filtering (the plain form)
-//   MT_STORAGE_F16   IEEE half volumes, half2 interpolation (precision form)
-//   MT_STORAGE_BF16  bfloat16 volumes, bfloat16x2 interpolation
+//   MT_STORAGE_F16   IEEE half volumes (precision form): the primary fetches
+//                    filtered in FP32, the cone-light fetches in half2
+//   MT_STORAGE_BF16  bfloat16 volumes, the cone-light fetches in bfloat16x2
 // Everything after the filtered texel (FBM, remaps, erosion, lighting,
 // accumulation) is FP32 in all three.  Each storage is instantiated by its own
 // translation unit (mt_march_u8.cu, mt_march_f16.cu, mt_march_bf16.cu).
@@ -13,26 +14,29 @@ namespace mt {
 
 // Storage-specific volume access.
 template <int S> struct Vol;
+// T3: the element of the 3D volumes (base, detail), T2: of the 2D images
+// (curl, weather), as build_march_args points at them.
 template <> struct Vol<MT_STORAGE_U8> {
-    using T = uint4;  // filter cells (launch_cells3 / launch_cells2)
-    template <int N> static MT_HD f4v tex3(const T* v, f3 s) { return tex3_u8<N>(v, s); }
-    template <int N> static MT_HD f4v tex3_light(const T* v, f3 s) { return tex3_u8_fused<N>(v, s); }
-    template <int N> static MT_HD f4v tex2(const T* v, float x, float y) { return tex2_u8<N>(v, x, y); }
+    using T3 = uint4;  // plane quads (launch_quads3)
+    using T2 = uint4;  // bilinear cells (launch_cells2)
+    template <int N> static MT_HD f4v tex3(const T3* v, f3 s) { return tex3_u8<N>(v, s); }
+    template <int N> static MT_HD f4v tex3_light(const T3* v, f3 s) { return tex3_u8_fused<N>(v, s); }
+    template <int N> static MT_HD f4v tex2(const T2* v, float x, float y) { return tex2_u8<N>(v, x, y); }
 };
-template <> struct Vol<MT_STORAGE_F16> {
-    using T = uint2;
-    template <int N> static MT_HD f4v tex3(const T* v, f3 s) { return tex3_p16<N, __half2>(v, s); }
-    template <int N> static MT_HD f4v tex3_light(const T* v, f3 s) { return tex3_p16<N, __half2>(v, s); }
-    template <int N> static MT_HD f4v tex2(const T* v, float x, float y) { return tex2_p16<N, __half2>(v, x, y); }
+// The 16-bit storages (P the packed pair type): the primary fetches (base at
+// the sample point, detail, curl, weather: the density that accumulates and
+// steers the march) filter the 16-bit texels in FP32; the six cone-light
+// fetches of an in-cloud step, which reach colour only, filter in the pair
+// type (half2 / bfloat16x2 lerps).
+template <class P> struct Vol16 {
+    using T3 = uint4;  // plane quads (launch_quads16)
+    using T2 = uint2;
+    template <int N> static MT_HD f4v tex3(const T3* v, f3 s) { return tex3_p16q_f32<N, P>(v, s); }
+    template <int N> static MT_HD f4v tex3_light(const T3* v, f3 s) { return tex3_p16q<N, P>(v, s); }
+    template <int N> static MT_HD f4v tex2(const T2* v, float x, float y) { return tex2_p16_f32<N, P>(v, x, y); }
 };
-template <> struct Vol<MT_STORAGE_BF16> {
-    using T = uint2;
-    template <int N> static MT_HD f4v tex3(const T* v, f3 s) { return tex3_p16<N, __nv_bfloat162>(v, s); }
-    template <int N> static MT_HD f4v tex3_light(const T* v, f3 s) { return tex3_p16<N, __nv_bfloat162>(v, s); }
-    template <int N> static MT_HD f4v tex2(const T* v, float x, float y) {
-        return tex2_p16<N, __nv_bfloat162>(v, x, y);
-    }
-};
+template <> struct Vol<MT_STORAGE_F16> : Vol16<__half2> {};
+template <> struct Vol<MT_STORAGE_BF16> : Vol16<__nv_bfloat162> {};
 
 struct Weather {
     float lo, mul, type;
@@ -42,11 +46,15 @@ struct Weather {
 };
 
 template <int S> struct Tex {
-    const typename Vol<S>::T* base;
-    const typename Vol<S>::T* detail;
-    const typename Vol<S>::T* curl;
-    const typename Vol<S>::T* weather;
+    const typename Vol<S>::T3* base;
+    const typename Vol<S>::T3* detail;
+    const typename Vol<S>::T2* curl;
+    const typename Vol<S>::T2* weather;
 };
+template <int S> MT_HD Tex<S> make_tex(const MarchArgs& a) {
+    return Tex<S>{(const typename Vol<S>::T3*)a.vol[0], (const typename Vol<S>::T3*)a.vol[1],
+                  (const typename Vol<S>::T2*)a.vol[2], (const typename Vol<S>::T2*)a.vol[3]};
+}
 
 template <int S> MT_HD Weather weather_at(const mt_params& p, const Frame& F, const Tex<S>& tx, f3 pos, f3 ec) {
     Weather w;
@@ -350,8 +358,7 @@ template <int G, int S, int BS, bool TR = false>
 __global__ void __launch_bounds__(BS, 1024 / BS) march_kernel(const __grid_constant__ MarchArgs a) {
     static_assert(G >= 1 && G <= 32 && (32 % G) == 0, "G must divide the warp");
     const Frame& F = a.frame;
-    using T = typename Vol<S>::T;
-    const Tex<S> tx{(const T*)a.vol[0], (const T*)a.vol[1], (const T*)a.vol[2], (const T*)a.vol[3]};
+    const Tex<S> tx = make_tex<S>(a);
     const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const unsigned idx = (unsigned)(tid / G);  // rays < 2^31 (images are at most 16384^2)
     const int lane = (int)(threadIdx.x % G);
@@ -391,7 +398,6 @@ __global__ void __launch_bounds__(BS, 1024 / BS) march_kernel(const __grid_const
 template <int G, int S>
 __global__ void __launch_bounds__(128, 8) march_batch_kernel(const __grid_constant__ BatchArgs b) {
     __shared__ int s_tile;
-    using T = typename Vol<S>::T;
     const int lane = (int)(threadIdx.x % G);
     const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
     constexpr int kRaysPerPass = 128 / G;
@@ -406,7 +412,7 @@ __global__ void __launch_bounds__(128, 8) march_batch_kernel(const __grid_consta
         const BatchTile tile = b.tiles[t];
         const MarchArgs& a = b.views[tile.view];
         const Frame& F = a.frame;
-        const Tex<S> tx{(const T*)a.vol[0], (const T*)a.vol[1], (const T*)a.vol[2], (const T*)a.vol[3]};
+        const Tex<S> tx = make_tex<S>(a);
         const bool full = (a.flags & MT_RENDER_FULL) != 0;
         const int id = a.time.frame_count_mod16;
         const int sx = full ? 0 : a.params.slot_x[id], sy = full ? 0 : a.params.slot_y[id];

@@ -263,22 +263,20 @@ __global__ void u8_to_16_kernel(const uint32_t* __restrict__ src, size_t n, uint
         (float)(v >> 24) / 255.0f);
 }
 
-// Filter-cell layout of an RGBA8 volume (what the plain form's samplers
-// read): cell (x, y, z) holds the eight texels a trilinear fetch at that cell
-// interpolates, x0 = x, x1 = (x + 1) mod N and so on (REPEAT), as two 16-byte
-// words -- {(x0,y0), (x1,y0), (x0,y1), (x1,y1)} at z0, then the same at z1 --
-// so one fetch reads one 32-byte sector.
-__global__ void cells3_kernel(const uint32_t* __restrict__ vol, int n, uint4* __restrict__ cells) {
+// Plane-quad layout of an RGBA8 volume (what the plain form's 3D samplers
+// read): entry (x, y, z) holds the four texels of plane z a trilinear fetch
+// at that cell interpolates, {(x0,y0), (x1,y0), (x0,y1), (x1,y1)} with
+// x1 = (x + 1) mod N, y1 likewise (REPEAT), as one 16-byte word: a fetch reads
+// two entries, at z0 and z1.
+__global__ void quads3_kernel(const uint32_t* __restrict__ vol, int n, uint4* __restrict__ quads) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const size_t nn = (size_t)n * n;
     if (i >= nn * n) return;
     const unsigned m = (unsigned)n - 1u;
     const unsigned x = (unsigned)(i % n), y = (unsigned)((i / n) % n), z = (unsigned)(i / nn);
-    const unsigned x1 = (x + 1u) & m, y1 = (y + 1u) & m, z1 = (z + 1u) & m;
-    const uint32_t* p0 = vol + (size_t)z * nn;
-    const uint32_t* p1 = vol + (size_t)z1 * nn;
-    cells[2 * i] = make_uint4(p0[y * n + x], p0[y * n + x1], p0[y1 * n + x], p0[y1 * n + x1]);
-    cells[2 * i + 1] = make_uint4(p1[y * n + x], p1[y * n + x1], p1[y1 * n + x], p1[y1 * n + x1]);
+    const unsigned x1 = (x + 1u) & m, y1 = (y + 1u) & m;
+    const uint32_t* p = vol + (size_t)z * nn;
+    quads[i] = make_uint4(p[y * n + x], p[y * n + x1], p[y1 * n + x], p[y1 * n + x1]);
 }
 
 // The same for an RGBA8 image (bilinear cells): {(x0,y0), (x1,y0), (x0,y1), (x1,y1)}.
@@ -291,11 +289,35 @@ __global__ void cells2_kernel(const uint32_t* __restrict__ img, int n, uint4* __
     cells[i] = make_uint4(img[y * n + x], img[y * n + x1], img[y1 * n + x], img[y1 * n + x1]);
 }
 
+// Plane-quad layout of a 16-bit volume (what the precision form's 3D samplers
+// read): entry (x, y, z) holds the four texels of the z plane a trilinear
+// fetch interpolates, as two 16-byte words {(x0,y0), (x1,y0)} and
+// {(x0,y1), (x1,y1)}, x1 = (x + 1) mod N (REPEAT): a fetch reads the entries
+// at z0 and z1, one 32-byte sector each.
+__global__ void quads16_kernel(const uint2* __restrict__ vol, int n, uint4* __restrict__ quads) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t nn = (size_t)n * n;
+    if (i >= nn * n) return;
+    const unsigned m = (unsigned)n - 1u;
+    const unsigned x = (unsigned)(i % n), y = (unsigned)((i / n) % n), z = (unsigned)(i / nn);
+    const unsigned x1 = (x + 1u) & m, y1 = (y + 1u) & m;
+    const uint2* p = vol + (size_t)z * nn;
+    const uint2 a = p[y * n + x], b = p[y * n + x1], c = p[y1 * n + x], d = p[y1 * n + x1];
+    quads[2 * i] = make_uint4(a.x, a.y, b.x, b.y);
+    quads[2 * i + 1] = make_uint4(c.x, c.y, d.x, d.y);
+}
+
 }  // namespace
 
-cudaError_t launch_cells3(const uint32_t* vol, int n, uint4* cells, cudaStream_t s) {
+cudaError_t launch_quads16(const uint2* vol, int n, uint4* quads, cudaStream_t s) {
     const size_t texels = (size_t)n * n * n;
-    cells3_kernel<<<(unsigned)((texels + 255) / 256), 256, 0, s>>>(vol, n, cells);
+    quads16_kernel<<<(unsigned)((texels + 255) / 256), 256, 0, s>>>(vol, n, quads);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_quads3(const uint32_t* vol, int n, uint4* quads, cudaStream_t s) {
+    const size_t texels = (size_t)n * n * n;
+    quads3_kernel<<<(unsigned)((texels + 255) / 256), 256, 0, s>>>(vol, n, quads);
     return cudaGetLastError();
 }
 cudaError_t launch_cells2(const uint32_t* img, int n, uint4* cells, cudaStream_t s) {

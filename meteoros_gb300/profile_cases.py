@@ -15,6 +15,10 @@ cases:
   godrays         1920x1080 god-ray radial blur
   tonemap         1920x1080 tone map + dither to RGBA8
   generate        noise-volume generation (gen_* kernels)
+  frame_fused     the 1080p reprojected frame with the reprojection fused into the TXAA
+                  resolve (resolve_kernel)
+  tga             a 128-slice stack of 128x128 run-length TGA files decoded on the device
+                  (tga_decode_kernel)
 
 Each case renders its frame `reps` times (default 2) so a profiler can skip
 the first launch and capture the next.
@@ -25,6 +29,29 @@ import argparse
 import sys
 
 SEED = 2017
+
+
+def _rle_tga(img) -> bytes:
+    """A 32-bit run-length TGA (image type 10, bottom-left origin) of an
+    (H, W, 4) RGBA8 image: runs of equal pixels as run packets, the rest as
+    raw packets of up to 128 pixels."""
+    h, w = img.shape[:2]
+    header = bytes([0, 0, 10, 0, 0, 0, 0, 0, 0, 0, 0, 0, w & 255, w >> 8, h & 255, h >> 8, 32, 8])
+    px = img[::-1].reshape(-1, 4)[:, [2, 1, 0, 3]]  # bottom row first, BGRA
+    out, i, n = [header], 0, len(px)
+    while i < n:
+        j = i + 1
+        while j < n and j - i < 128 and (px[j] == px[i]).all():
+            j += 1
+        if j - i > 1:
+            out.append(bytes([0x80 | (j - i - 1)]) + px[i].tobytes())
+        else:
+            j = i + 1
+            while j < n and j - i < 128 and not (j + 1 < n and (px[j] == px[j + 1]).all()):
+                j += 1
+            out.append(bytes([j - i - 1]) + px[i:j].tobytes())
+        i = j
+    return b"".join(out)
 
 
 def main(argv=None) -> int:
@@ -57,7 +84,9 @@ def main(argv=None) -> int:
                 ctx.render(cam, old, tm, params, prev, cur, None, abi.MT_RENDER_CHECKERBOARD)
             else:
                 ctx.txaa(cam, old, tm, params, prev, cur, out)
-    elif a.case == "frame":
+    elif a.case in ("frame", "frame_fused"):
+        if a.case == "frame_fused":
+            ctx.set_tuning(fused_resolve=True)
         W, H = 1920, 1080
         seq = scenes.config_sequence(SEED, W, H, frames=a.reps)
         prev = torch.rand((H, W, 4), device=dev)
@@ -107,6 +136,18 @@ def main(argv=None) -> int:
     elif a.case == "generate":
         for r in range(a.reps):
             ctx.generate_volumes(SEED + r)
+    elif a.case == "tga":
+        import ctypes as C
+
+        base = ctx.download_volumes()["base"]
+        files = [_rle_tga(base[z]) for z in range(abi.MT_BASE_N)]
+        arr = (C.c_void_p * len(files))(*[C.cast(C.c_char_p(f), C.c_void_p) for f in files])
+        sizes = (C.c_size_t * len(files))(*[len(f) for f in files])
+        for _ in range(a.reps):
+            st = ctx.lib.mt_decode_tga_volume(ctx.handle, abi.MT_VOLUME_BASE, arr, sizes, len(files), None)
+            if st != abi.MT_OK:
+                print(ctx.lib.mt_last_error(ctx.handle).decode(), file=sys.stderr)
+                return 1
     else:
         print(f"unknown case {a.case}", file=sys.stderr)
         return 2

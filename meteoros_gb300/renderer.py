@@ -155,7 +155,8 @@ class Context:
     def set_tuning(self, march_lanes: int | None = None, fused_resolve: bool | None = None,
                    batch_tile: tuple[int, int] | None = None, batch_lanes: int | None = None,
                    batch_direct: bool | None = None, reproject_serial: bool | None = None,
-                   march_block: int | None = None, march_order: int | None = None) -> abi.Tuning:
+                   march_block: int | None = None, march_order: int | None = None,
+                   batch_order: int | None = None) -> abi.Tuning:
         t = abi.Tuning()
         self._check(self.lib.mt_get_tuning(self.handle, C.byref(t)))
         if march_lanes is not None:
@@ -174,6 +175,8 @@ class Context:
             t.march_block = march_block
         if march_order is not None:
             t.march_order = march_order
+        if batch_order is not None:
+            t.batch_order = batch_order
         self._check(self.lib.mt_set_tuning(self.handle, C.byref(t)))
         return t
 

@@ -57,9 +57,9 @@ def per_view(ctx, bufs):
 def test_batch_equals_per_view(ctx, storage):
     views, bufs = build_views(storage)
     want, st_want = per_view(ctx, bufs)
-    for tile, lanes, direct in (((16, 8), 1, False), ((8, 8), 4, False), ((32, 8), 8, False),
-                                ((16, 8), 1, True), ((16, 16), 4, True)):
-        ctx.set_tuning(batch_tile=tile, batch_lanes=lanes, batch_direct=direct)
+    for tile, lanes, direct, order in (((16, 8), 1, False, 0), ((8, 8), 4, False, 1), ((32, 8), 8, False, 0),
+                                       ((16, 8), 1, True, 1), ((16, 16), 4, True, 0)):
+        ctx.set_tuning(batch_tile=tile, batch_lanes=lanes, batch_direct=direct, batch_order=order)
         for b in bufs:
             b[4].fill_(float("nan"))
             b[5].fill_(float("nan"))
@@ -70,7 +70,7 @@ def test_batch_equals_per_view(ctx, storage):
             assert_bits_equal(b[5].cpu().numpy(), wm, f"view {i} mask, tile {tile} lanes {lanes}")
         assert (st.primary_samples, st.light_samples, st.marched_rays, st.pixels) == (
             st_want.primary_samples, st_want.light_samples, st_want.marched_rays, st_want.pixels)
-    ctx.set_tuning(batch_tile=(16, 8), batch_lanes=1, batch_direct=False)
+    ctx.set_tuning(batch_tile=(16, 8), batch_lanes=1, batch_direct=False, batch_order=0)
 
 
 def test_autotune_keeps_results(ctx):
@@ -78,14 +78,14 @@ def test_autotune_keeps_results(ctx):
     want, _ = per_view(ctx, bufs)
     best = ctx.autotune_batch(views)
     assert (best.batch_tile_w, best.batch_tile_h) in ((8, 8), (16, 8), (16, 16), (32, 8))
-    assert best.batch_lanes in (1, 4)
+    assert best.batch_lanes in (1, 4, 8) and best.batch_order in (0, 1)
     for b in bufs:
         b[4].fill_(float("nan"))
     ctx.render_batch(views)
     ctx.stats(reset=True)
     for i, (b, (wc, _)) in enumerate(zip(bufs, want)):
         assert_bits_equal(b[4].cpu().numpy(), wc, f"view {i} after autotune")
-    ctx.set_tuning(batch_tile=(16, 8), batch_lanes=1)
+    ctx.set_tuning(batch_tile=(16, 8), batch_lanes=1, batch_order=0)
 
 
 def test_batch_rejects_mixed_storage_and_bad_views(ctx):
