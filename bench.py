@@ -55,9 +55,11 @@ FLUSH_BYTES = 256 << 20
 FLOPS_PER_PIXEL, FLOPS_PER_RAY, FLOPS_PER_PRIMARY, FLOPS_PER_LIGHT = 132.6, 506.5, 307.8, 229.6
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one march_kernel<4>
 # launch on this workload's 1080p checkerboard frame, from one ncu capture with
-# cold caches (the bench flushes L2 before every frame too); the colour and
-# mask writes are still in L2 when the launch ends.
-MARCH_DRAM_BYTES_PER_LAUNCH = 8992000 + 417024
+# cold caches (the bench flushes L2 before every frame too): one read of the
+# volumes in the samplers' layout (plane quads of the base and detail
+# volumes, bilinear cells of the curl and weather maps, ~37 MB) and the part
+# of the colour and mask writes that leaves L2 during the launch.
+MARCH_DRAM_BYTES_PER_LAUNCH = 34119424 + 1912576
 
 
 def parse():
@@ -655,8 +657,10 @@ def run_gb300(args) -> int:
                      "peak": hbm_peak, "unit": "GB/s", "frac": round(achieved / hbm_peak, 5),
                      "traffic": MARCH_DRAM_BYTES_PER_LAUNCH, "algorithmic_bytes": march_bytes,
                      "peak_source": peak_src,
-                     "note": "the raymarch is FP32/L1-texel bound, not HBM bound: its HBM bytes are the colour and "
-                             "mask writes plus one read of the noise volumes"},
+                     "note": "the raymarch is FP32-issue and texel-latency bound, not HBM bound: its algorithmic HBM "
+                             "bytes are the colour and mask writes plus one read of the 9.5 MB of RGBA8 volumes; "
+                             "the traffic is one read of the samplers' layout of them (plane quads: each texel "
+                             "stored four times, for 2 loads per trilinear fetch instead of 8)"},
         "roofline_fp32": {"bound": "fp32", "kernel": "march_kernel",
                           "achieved": round(march_flops / (march_ms * 1e-3) / 1e12, 3), "peak": round(fp32_peak, 2),
                           "unit": "TFLOP/s", "frac": round(march_flops / (march_ms * 1e-3) / 1e12 / fp32_peak, 4),
