@@ -81,7 +81,9 @@ MT_HD float div_ieee(float a, float b) { return a / b; }
 #else
 static __device__ __noinline__ float div_ieee(float a, float b) { return a / b; }
 #endif
-MT_HD Rcp make_rcp(float b) { return Rcp{b, div_ieee(1.0f, b)}; }
+// The reciprocal of a denominator: __frcp_rn is the IEEE round-to-nearest-even
+// reciprocal, RN(1/b) -- the value 1.0f / b gives -- inline, without the call.
+MT_HD Rcp make_rcp(float b) { return Rcp{b, __frcp_rn(b)}; }
 MT_HD float rdiv_core(float a, Rcp r) {
     const float q0 = __fmul_rn(a, r.y);
     return __fmaf_rn(__fmaf_rn(-q0, r.b, a), r.y, q0);
