@@ -292,11 +292,16 @@ template <> struct Pair<__half2> {
     static MT_HD __half2 from_bits(uint32_t u) { return *reinterpret_cast<__half2*>(&u); }
     static MT_HD __half2 splat(float f) { return __float2half2_rn(f); }
     static MT_HD float2 to_float2(__half2 h) { return __half22float2(h); }
+    // (a.low, b.low) and (a.high, b.high)
+    static MT_HD __half2 lows(__half2 a, __half2 b) { return __lows2half2(a, b); }
+    static MT_HD __half2 highs(__half2 a, __half2 b) { return __highs2half2(a, b); }
 };
 template <> struct Pair<__nv_bfloat162> {
     static MT_HD __nv_bfloat162 from_bits(uint32_t u) { return *reinterpret_cast<__nv_bfloat162*>(&u); }
     static MT_HD __nv_bfloat162 splat(float f) { return __float2bfloat162_rn(f); }
     static MT_HD float2 to_float2(__nv_bfloat162 h) { return __bfloat1622float2(h); }
+    static MT_HD __nv_bfloat162 lows(__nv_bfloat162 a, __nv_bfloat162 b) { return __lows2bfloat162(a, b); }
+    static MT_HD __nv_bfloat162 highs(__nv_bfloat162 a, __nv_bfloat162 b) { return __highs2bfloat162(a, b); }
 };
 
 template <class P> struct PairTexel {
@@ -324,7 +329,12 @@ template <class P> MT_HD PairTexel<P> pair_lo(uint4 q) {
 template <class P> MT_HD PairTexel<P> pair_hi(uint4 q) {
     return PairTexel<P>{Pair<P>::from_bits(q.z), Pair<P>::from_bits(q.w)};
 }
+template <int N, class P> MT_HD PairTexel<P> tex3_p16q_pairs(const uint4* __restrict__ quads, f3 s);
 template <int N, class P> MT_HD f4v tex3_p16q(const uint4* __restrict__ quads, f3 s) {
+    return pair_to_f4(tex3_p16q_pairs<N, P>(quads, s));
+}
+// The filtered texel as its two pairs, (r, g) and (b, a), in the pair type.
+template <int N, class P> MT_HD PairTexel<P> tex3_p16q_pairs(const uint4* __restrict__ quads, f3 s) {
     constexpr unsigned M = (unsigned)N - 1u;
     const float fn = (float)N;
     float u = s.x * fn - 0.5f, v = s.y * fn - 0.5f, w = s.z * fn - 0.5f;
@@ -339,7 +349,7 @@ template <int N, class P> MT_HD f4v tex3_p16q(const uint4* __restrict__ quads, f
     PairTexel<P> c10 = lerp_pair(pair_lo<P>(e01), pair_hi<P>(e01), a);
     PairTexel<P> c01 = lerp_pair(pair_lo<P>(e10), pair_hi<P>(e10), a);
     PairTexel<P> c11 = lerp_pair(pair_lo<P>(e11), pair_hi<P>(e11), a);
-    return pair_to_f4(lerp_pair(lerp_pair(c00, c10, b), lerp_pair(c01, c11, b), g));
+    return lerp_pair(lerp_pair(c00, c10, b), lerp_pair(c01, c11, b), g);
 }
 
 // The same fetch with FP32 weights and FP32 lerps of the 16-bit texel values

@@ -2,11 +2,15 @@
 // per ray and on the storage of the noise volumes:
 //   MT_STORAGE_U8    RGBA8 volumes, exact FP32 filtering (the plain form)
 //   MT_STORAGE_F16   IEEE half volumes (precision form): the primary fetches
-//                    filtered in FP32, the cone-light fetches in half2
-//   MT_STORAGE_BF16  bfloat16 volumes, the cone-light fetches in bfloat16x2
-// Everything after the filtered texel (FBM, remaps, erosion, lighting,
-// accumulation) is FP32 in all three.  Each storage is instantiated by its own
-// translation unit (mt_march_u8.cu, mt_march_f16.cu, mt_march_bf16.cu).
+//                    filtered in FP32; the cone-light samples' filtering and
+//                    density math (FBM, remaps, coverage) in half2, two
+//                    samples per pair
+//   MT_STORAGE_BF16  bfloat16 volumes, the cone-light fetches filtered in
+//                    bfloat16x2
+// Apart from the FP16 form's cone-light density math, everything after the
+// filtered texel (FBM, remaps, erosion, lighting, transmittance, radiance,
+// accumulation) is FP32.  Each storage is instantiated by its own translation
+// unit (mt_march_u8.cu, mt_march_f16.cu, mt_march_bf16.cu).
 #pragma once
 #include "mt_shared.cuh"
 
@@ -27,7 +31,8 @@ template <> struct Vol<MT_STORAGE_U8> {
 // the sample point, detail, curl, weather: the density that accumulates and
 // steers the march) filter the 16-bit texels in FP32; the six cone-light
 // fetches of an in-cloud step, which reach colour only, filter in the pair
-// type (half2 / bfloat16x2 lerps).
+// type (half2 / bfloat16x2 lerps; FP16 also runs their density math in half2,
+// sample_light_pair).
 template <class P> struct Vol16 {
     using T3 = uint4;  // plane quads (launch_quads16)
     using T2 = uint2;
@@ -107,6 +112,32 @@ MT_HD float sample_light(const mt_params& p, const Tex<S>& tx, f3 point, const W
     const float v = fminf(fmaxf(baseCloud, wt.lo), 1.0f);
     const float bc = fminf(fmaxf((v - wt.lo) * wt.r_lo.y, 0.0f), 1.0f);
     return bc * wt.mul;
+}
+
+// Two cone-light samples at once in the pair type (FP16 storage): sample i in
+// the low half, sample i + 1 in the high half.  Each sample's filtered texel,
+// FBM, base-shape remap, height gradient and coverage remap --
+// sample_light's steps, with the division by a reciprocal -- run as half2
+// arithmetic; the results return to FP32 for the erosion and the accumulation
+// of the light density.  (bfloat16's 8-bit mantissa is too coarse for the
+// remaps: the bfloat16 form filters in pairs and does this math in FP32.)
+template <class P>
+MT_HD float2 sample_light_pair(const mt_params& p, const uint4* base, f3 s0, f3 s1, const Weather& wt) {
+    using Q = Pair<P>;
+    const PairTexel<P> n0 = tex3_p16q_pairs<MT_BASE_N, P>(base, s0);
+    const PairTexel<P> n1 = tex3_p16q_pairs<MT_BASE_N, P>(base, s1);
+    const P x = Q::lows(n0.rg, n1.rg), y = Q::highs(n0.rg, n1.rg);
+    const P z = Q::lows(n0.ba, n1.ba), w = Q::highs(n0.ba, n1.ba);
+    const P zero = Q::splat(0.0f), one = Q::splat(1.0f);
+    P fbm = __hfma2(w, Q::splat(0.125f), __hfma2(z, Q::splat(0.25f), __hmul2(y, Q::splat(0.625f))));
+    fbm = __hmin2(__hmax2(fbm, zero), one);
+    const P lo = __hsub2(fbm, Q::splat(0.9f));
+    P bc = __hmin2(__hmax2(__hmul2(__hsub2(x, lo), h2rcp(__hsub2(one, lo))), zero), one);
+    if (p.height_gradient) bc = __hmul2(bc, Q::splat(wt.hgrad));
+    const P wlo = Q::splat(wt.lo);
+    const P v = __hmin2(__hmax2(bc, wlo), one);
+    bc = __hmin2(__hmax2(__hmul2(__hsub2(v, wlo), Q::splat(wt.r_lo.y)), zero), one);
+    return Q::to_float2(__hmul2(bc, Q::splat(wt.mul)));
 }
 
 // cloudRayMarch.comp:542-563.  The texture part is the same for the primary
@@ -206,14 +237,32 @@ MT_HD StepOut eval_step(const mt_params& p, const Frame& F, const Tex<S>& tx, co
         // inlines this, whatever the compiler's contraction setting.
         const f3 pb = pos - f3{F.ec[0], F.inner_alt, F.ec[2]};
         const f3 prel{__fmul_rn(pb.x, F.r_thick.y), __fmul_rn(pb.y, F.r_thick.y), __fmul_rn(pb.z, F.r_thick.y)};
-#pragma unroll 1
-        for (int i = 0; i < 6; ++i) {
+        auto light_point = [&](int i) {
             const f3 k = rc.koff[i];
-            const f3 slp{__fadd_rn(prel.x, k.x), __fadd_rn(prel.y, k.y), __fadd_rn(prel.z, k.z)};
-            const float cbl = sample_light<S>(p, tx, slp, wt);
-            if (cbl > 0.0f) {
-                dl = fmaf(fmaf(1.5f, cbl, -ero.lo), ero.r.y, dl);  // erode(1.5 * cbl)
-                if (TR) o.code |= 32 << i;
+            return f3{__fadd_rn(prel.x, k.x), __fadd_rn(prel.y, k.y), __fadd_rn(prel.z, k.z)};
+        };
+        if constexpr (S != MT_STORAGE_F16) {
+#pragma unroll 1
+            for (int i = 0; i < 6; ++i) {
+                const float cbl = sample_light<S>(p, tx, light_point(i), wt);
+                if (cbl > 0.0f) {
+                    dl = fmaf(fmaf(1.5f, cbl, -ero.lo), ero.r.y, dl);  // erode(1.5 * cbl)
+                    if (TR) o.code |= 32 << i;
+                }
+            }
+        } else {
+            // FP16 storage: two samples at a time, density math in half2
+#pragma unroll 1
+            for (int i = 0; i < 6; i += 2) {
+                const float2 cbl = sample_light_pair<__half2>(p, tx.base, light_point(i), light_point(i + 1), wt);
+                if (cbl.x > 0.0f) {
+                    dl = fmaf(fmaf(1.5f, cbl.x, -ero.lo), ero.r.y, dl);
+                    if (TR) o.code |= 32 << i;
+                }
+                if (cbl.y > 0.0f) {
+                    dl = fmaf(fmaf(1.5f, cbl.y, -ero.lo), ero.r.y, dl);
+                    if (TR) o.code |= 32 << (i + 1);
+                }
             }
         }
         o.E = light_energy(relH, dl, baseDensity, rc.HG_light, rc.cos_q, 5.0f);

@@ -2,8 +2,11 @@
 
 3840x2160, one full-raymarch frame, 128 primary + 6 light steps.  Forms:
   plain     RGBA8 volumes, exact FP32 (the parity form)
-  fp16      IEEE-half volumes, half2 interpolation, FP64 shell intersection
-  bf16      bfloat16 volumes, bfloat16x2 interpolation, FP64 shell intersection
+  fp16      IEEE-half volumes; primary density filtered in FP32, the cone-light
+            samples' filtering and density math in half2; FP64 shell
+            intersection
+  bf16      bfloat16 volumes; the cone-light samples filtered in bfloat16x2;
+            FP64 shell intersection
 Each is compared with the FP64 oracle fed the texel values that form stores,
 on a 1/64 sample of the pixels (every 8th column and row).
 
