@@ -5,8 +5,7 @@
 //                    filtered in FP32; the cone-light samples' filtering and
 //                    density math (FBM, remaps, coverage) in half2, two
 //                    samples per pair
-//   MT_STORAGE_BF16  bfloat16 volumes, the cone-light fetches filtered in
-//                    bfloat16x2
+//   MT_STORAGE_BF16  bfloat16 volumes, filtered in FP32 (a storage form)
 // Apart from the FP16 form's cone-light density math, everything after the
 // filtered texel (FBM, remaps, erosion, lighting, transmittance, radiance,
 // accumulation) is FP32.  Each storage is instantiated by its own translation
@@ -27,17 +26,16 @@ template <> struct Vol<MT_STORAGE_U8> {
     template <int N> static MT_HD f4v tex3_light(const T3* v, f3 s) { return tex3_u8_fused<N>(v, s); }
     template <int N> static MT_HD f4v tex2(const T2* v, float x, float y) { return tex2_u8<N>(v, x, y); }
 };
-// The 16-bit storages (P the packed pair type): the primary fetches (base at
-// the sample point, detail, curl, weather: the density that accumulates and
-// steers the march) filter the 16-bit texels in FP32; the six cone-light
-// fetches of an in-cloud step, which reach colour only, filter in the pair
-// type (half2 / bfloat16x2 lerps; FP16 also runs their density math in half2,
-// sample_light_pair).
+// The 16-bit storages (P the packed pair type): every fetch filters the
+// 16-bit texels in FP32, except the FP16 form's six cone-light samples per
+// in-cloud step, which reach colour only and run in half2 (lerps and density
+// math, sample_light_pair).
 template <class P> struct Vol16 {
     using T3 = uint4;  // plane quads (launch_quads16)
     using T2 = uint2;
     template <int N> static MT_HD f4v tex3(const T3* v, f3 s) { return tex3_p16q_f32<N, P>(v, s); }
-    template <int N> static MT_HD f4v tex3_light(const T3* v, f3 s) { return tex3_p16q<N, P>(v, s); }
+    // bfloat16 (an 8-bit mantissa) filters its cone-light samples in FP32 too
+    template <int N> static MT_HD f4v tex3_light(const T3* v, f3 s) { return tex3_p16q_f32<N, P>(v, s); }
     template <int N> static MT_HD f4v tex2(const T2* v, float x, float y) { return tex2_p16_f32<N, P>(v, x, y); }
 };
 template <> struct Vol<MT_STORAGE_F16> : Vol16<__half2> {};
@@ -119,8 +117,8 @@ MT_HD float sample_light(const mt_params& p, const Tex<S>& tx, f3 point, const W
 // FBM, base-shape remap, height gradient and coverage remap --
 // sample_light's steps, with the division by a reciprocal -- run as half2
 // arithmetic; the results return to FP32 for the erosion and the accumulation
-// of the light density.  (bfloat16's 8-bit mantissa is too coarse for the
-// remaps: the bfloat16 form filters in pairs and does this math in FP32.)
+// of the light density.  (bfloat16's 8-bit mantissa is too coarse for this:
+// the bfloat16 form does its cone-light samples in FP32.)
 template <class P>
 MT_HD float2 sample_light_pair(const mt_params& p, const uint4* base, f3 s0, f3 s1, const Weather& wt) {
     using Q = Pair<P>;

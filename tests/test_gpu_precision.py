@@ -5,8 +5,7 @@
   fp16      IEEE-half volumes; primary density filtered in FP32, the cone-light
             samples' filtering and density math in half2; FP64 shell
             intersection
-  bf16      bfloat16 volumes; the cone-light samples filtered in bfloat16x2;
-            FP64 shell intersection
+  bf16      bfloat16 volumes, filtered in FP32; FP64 shell intersection
 Each is compared with the FP64 oracle fed the texel values that form stores,
 on a 1/64 sample of the pixels (every 8th column and row).
 
@@ -23,8 +22,7 @@ fraction are reported.
 The bar is 2e-3 relative to max(1, |value|): absolute below 1, relative above.
 HDR cloud colours reach 40, where an absolute 2e-3 would be a 5e-5 relative
 bar, finer than the reference's own RGBA16F images hold (a step of 2^-11
-relative).  bfloat16 (an 8-bit mantissa: the interpolation weights alone
-carry 2^-9) is held to 1e-2 on the same scale.
+relative).
 """
 import numpy as np
 import pytest
@@ -36,7 +34,7 @@ pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
 
 W, H, STRIDE = 3840, 2160, 8
-BAR = {"plain": 2e-3, "fp16": 2e-3, "bf16": 1e-2}
+BAR = {"plain": 2e-3, "fp16": 2e-3, "bf16": 2e-3}
 
 
 def split_stats(gpu_rgb, ref_rgb, same):
