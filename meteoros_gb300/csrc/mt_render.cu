@@ -235,12 +235,24 @@ __global__ void __launch_bounds__(kTxaaTW * kTxaaTH, 4) txaa_kernel(const __grid
     const int x = blockIdx.x * kTxaaTW + threadIdx.x;
     const int ya = blockIdx.y * TH + threadIdx.y;
     bool plain = true;
-    for (int i = tid; i < SW * SH; i += kTxaaTW * kTxaaTH) {
+    // every load of the tile in flight before the first shared-memory store
+    constexpr int NT = kTxaaTW * kTxaaTH, NL = (SW * SH + NT - 1) / NT;
+    float4 c[NL];
+#pragma unroll
+    for (int k = 0; k < NL; ++k) {
+        const int i = tid + k * NT;
         const int gx = x0 + i % SW, gy = y0 + i / SW;
-        const float4 c = (gx >= 0 && gy >= 0 && gx < W && gy < H) ? __ldg(a.current + (size_t)gy * (size_t)W + (size_t)gx)
-                                                                  : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        plain = plain & txaa_plain(c);
-        tile[i / SW][i % SW] = c;
+        c[k] = (i < SW * SH && gx >= 0 && gy >= 0 && gx < W && gy < H)
+                   ? __ldg(a.current + (size_t)gy * (size_t)W + (size_t)gx)
+                   : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+#pragma unroll
+    for (int k = 0; k < NL; ++k) {
+        const int i = tid + k * NT;
+        if (i < SW * SH) {
+            plain = plain & txaa_plain(c[k]);
+            tile[i / SW][i % SW] = c[k];
+        }
     }
     // the whole tile non-negative and NaN-free: the block takes the min/max path
     plain = __syncthreads_and(plain) != 0;

@@ -12,6 +12,11 @@ cases:
   batch           64-view batched raymarch (march_batch_kernel), RGBA8 volumes
   batch_fp16      the same with FP16 volumes
   precision       3840x2160 full frame, FP16 volumes (march_kernel<1>, half2 path)
+  precision_bf16  the same frame with bfloat16 volumes (filtered in FP32)
+  upload          host RGBA8 volumes uploaded: the 16-bit copies (u8_to_16_kernel) and the
+                  samplers' layouts (quads3_kernel, quads16_kernel, cells2_kernel)
+  batch_noalloc   16 views through the allocation-free batch entry (noalloc_store_kernel,
+                  noalloc_tiles_kernel, march_batch_kernel)
   godrays         1920x1080 god-ray radial blur
   tonemap         1920x1080 tone map + dither to RGBA8
   generate        noise-volume generation (gen_* kernels)
@@ -111,10 +116,10 @@ def main(argv=None) -> int:
             views.append(scenes.make_view(cam, cam, tm, params, cur, None, None, abi.MT_RENDER_FULL))
         for _ in range(a.reps):
             ctx.render_batch(views)
-    elif a.case == "precision":
+    elif a.case in ("precision", "precision_bf16"):
         W, H = 3840, 2160
         cam, tm, params, _ = scenes.config_view(SEED + 2, W, H)
-        params.storage = abi.MT_STORAGE_F16
+        params.storage = abi.MT_STORAGE_BF16 if a.case == "precision_bf16" else abi.MT_STORAGE_F16
         params.fp64_shells = 1
         cur = torch.empty((H, W, 4), device=dev)
         for _ in range(a.reps):
@@ -133,6 +138,30 @@ def main(argv=None) -> int:
                 ctx.godrays(cam, (1.0, 1.0, 0.57, 1.0), mask, img, out)
             else:
                 ctx.tonemap(tm, img, out8, abi.MT_LDR_RGBA8)
+    elif a.case == "upload":
+        # host RGBA8 volumes in: the 16-bit copies and the samplers' layouts rebuilt
+        vols = ctx.download_volumes()
+        for _ in range(a.reps):
+            ctx.upload_volumes(vols["base"], vols["detail"], vols["curl"], vols["weather"])
+    elif a.case == "batch_noalloc":
+        import ctypes as C
+
+        # 16 views at the two smaller config-3 sizes: within the entry's fixed tile table
+        specs = scenes.config3_views(SEED, n_views=16, resolutions=((256, 256), (640, 360)))
+        for v in range(16):
+            ctx.generate_weather(v, SEED + v)
+        views, keep = [], []
+        for w, h, cam, tm, params in specs:
+            cur = torch.empty((h, w, 4), device=dev)
+            keep.append(cur)
+            views.append(scenes.make_view(cam, cam, tm, params, cur, None, None, abi.MT_RENDER_FULL))
+        arr = (abi.View * len(views))(*views)
+        stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+        for _ in range(a.reps):
+            st = ctx.lib.mt_render_batch_noalloc(ctx.handle, arr, len(views), stream)
+            if st != abi.MT_OK:
+                print(ctx.lib.mt_last_error(ctx.handle).decode(), file=sys.stderr)
+                return 1
     elif a.case == "generate":
         for r in range(a.reps):
             ctx.generate_volumes(SEED + r)
