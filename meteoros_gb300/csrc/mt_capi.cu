@@ -1054,13 +1054,17 @@ struct NoallocStore {
 };
 static_assert(sizeof(NoallocStore) <= 32000, "kernel parameter space");
 
-// Copies n_views view tables into the array at view first_view; the launch
-// holding view 0 also zeroes the work counter.
+// Copies n_views view tables into the array at view first_view, one CTA a
+// view (a warp's parameter-space reads at 32 different words are served one
+// word at a time, so the copies are spread over SMs); the launch holding
+// view 0 also zeroes the work counter.
 __global__ void noalloc_store_kernel(const __grid_constant__ NoallocStore p, unsigned char* scratch) {
-    uint32_t* dst = reinterpret_cast<uint32_t*>(scratch + kNoallocViewsOff) + (size_t)p.first_view * kViewWords;
-    const int n = p.n_views * kViewWords;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = p.words[i];
-    if (p.first_view == 0 && threadIdx.x == 0) *reinterpret_cast<unsigned*>(scratch) = 0u;
+    const int v = blockIdx.x;
+    if (v >= p.n_views) return;
+    uint32_t* dst = reinterpret_cast<uint32_t*>(scratch + kNoallocViewsOff) + (size_t)(p.first_view + v) * kViewWords;
+    const uint32_t* src = p.words + (size_t)v * kViewWords;
+    for (int i = threadIdx.x; i < kViewWords; i += blockDim.x) dst[i] = src[i];
+    if (p.first_view == 0 && v == 0 && threadIdx.x == 0) *reinterpret_cast<unsigned*>(scratch) = 0u;
 }
 
 // The tile list's description: views in hand-out order with their ray grids
@@ -1194,7 +1198,7 @@ MT_API mt_status mt_render_batch_noalloc(mt_ctx* ctx, const mt_view* views, int 
             // the view's reprojection reads nothing of the array: launched as its table is built
             if (!(a.flags & MT_RENDER_FULL)) MT_CUDA(ctx, mt::launch_reproject(a, s));
         }
-        noalloc_store_kernel<<<1, 256, 0, s>>>(store, dev);
+        noalloc_store_kernel<<<store.n_views, 256, 0, s>>>(store, dev);
         MT_CUDA(ctx, cudaGetLastError());
     }
     if (n_tiles == 0) return MT_OK;
