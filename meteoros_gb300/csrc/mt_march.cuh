@@ -336,10 +336,11 @@ MT_HD f3 ray_march_group(const mt_params& p, const Frame& F, const Tex<S>& tx, c
 }
 
 // cloudRayMarch.comp:690-826 for one pixel, marched by a group of G lanes;
-// lane 0 stores.
+// lane 0 stores.  `jitter`: the view's per-step jitter table (a.jitter, or a
+// copy of it in shared memory).
 template <int G, int S, bool TR = false>
 MT_HD void march_pixel(const MarchArgs& a, const Frame& F, const Tex<S>& tx, int px, int py, Counts& cnt,
-                       unsigned gmask, int lane) {
+                       unsigned gmask, int lane, const float (*jitter)[3]) {
     const mt_params& p = a.params;
     const int W = a.width, H = a.height;
     const int pixelID = a.time.frame_count_mod16;
@@ -384,7 +385,7 @@ MT_HD void march_pixel(const MarchArgs& a, const Frame& F, const Tex<S>& tx, int
     }
     float accum = 0.0f;
     if (TR) cnt.sig = 2166136261u;
-    f3 res = ray_march_group<G, S, TR>(p, F, tx, a.time, a.jitter, ray.direction, in.point, in.t, out.t, accum, cnt,
+    f3 res = ray_march_group<G, S, TR>(p, F, tx, a.time, jitter, ray.direction, in.point, in.t, out.t, accum, cnt,
                                        gmask, lane);
     if (lane != 0) return;
     float godAccum = accum;
@@ -401,6 +402,10 @@ MT_HD void march_pixel(const MarchArgs& a, const Frame& F, const Tex<S>& tx, int
 // block's slot pixel.  Full: one ray per pixel.  G consecutive lanes (an
 // aligned segment of a warp) march one ray.  BS threads per CTA (256 by
 // default, 128 or 32 selectable), 64 registers a thread in every case.
+// Every step reads its jitter vector at an index taken from int(t), which
+// differs from lane to lane: from the parameter space a warp's reads at up to
+// 16 different words are served one word at a time, from shared memory in one
+// pass (48 words, 3 apart: distinct banks), so the table is copied there.
 template <int G, int S, int BS, bool TR = false>
 __global__ void __launch_bounds__(BS, 1024 / BS) march_kernel(const __grid_constant__ MarchArgs a) {
     static_assert(G >= 1 && G <= 32 && (32 % G) == 0, "G must divide the warp");
@@ -410,6 +415,9 @@ __global__ void __launch_bounds__(BS, 1024 / BS) march_kernel(const __grid_const
     const unsigned idx = (unsigned)(tid / G);  // rays < 2^31 (images are at most 16384^2)
     const int lane = (int)(threadIdx.x % G);
     const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
+    __shared__ float s_jitter[16][3];
+    for (int i = threadIdx.x; i < 48; i += BS) (&s_jitter[0][0])[i] = (&a.jitter[0][0])[i];
+    __syncthreads();
     Counts cnt{0u, 0u, 0u};
     unsigned pixels = 0;
     int px = 0, py = 0;
@@ -430,7 +438,7 @@ __global__ void __launch_bounds__(BS, 1024 / BS) march_kernel(const __grid_const
         }
     }
     if (active) {
-        march_pixel<G, S, TR>(a, F, tx, px, py, cnt, gmask, lane);
+        march_pixel<G, S, TR>(a, F, tx, px, py, cnt, gmask, lane, s_jitter);
         pixels = lane == 0 ? 1u : 0u;
     }
     if (a.stats) flush_counts(a.stats, cnt, pixels);
@@ -471,7 +479,7 @@ __global__ void __launch_bounds__(128, 8) march_batch_kernel(const __grid_consta
             const int px = rx * step + sx, py = ry * step + sy;
             const bool active = r < tile_rays && rx < tile.nrx && ry < tile.nry && px < a.width && py < a.height;
             if (active) {
-                march_pixel<G, S>(a, F, tx, px, py, cnt, gmask, lane);
+                march_pixel<G, S>(a, F, tx, px, py, cnt, gmask, lane, a.jitter);
                 pixels += lane == 0 ? 1u : 0u;
             }
         }
