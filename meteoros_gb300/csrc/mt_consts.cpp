@@ -100,6 +100,14 @@ void make_march_frame(Frame* f, const mt_params& p, const mt_camera_ubo& cam, co
     f->ec[0] = f->eye[0];
     f->ec[1] = -f->R;
     f->ec[2] = f->eye[2];
+    // ray_sphere_fp64's origin terms, in its order of operations
+    const float radii[2] = {f->Rin, f->Rout};
+    for (int s = 0; s < 2; ++s) {
+        const double r = (double)radii[s];
+        for (int i = 0; i < 3; ++i) f->sh_o[s][i] = ((double)f->eye[i] - (double)f->ec[i]) / r;
+        const double* o = f->sh_o[s];
+        f->sh_c[s] = (o[0] * o[0] + o[1] * o[1] + o[2] * o[2]) - 1.0;
+    }
 }
 
 }  // namespace mt

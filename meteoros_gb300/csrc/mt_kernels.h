@@ -43,6 +43,11 @@ struct Frame {
     float ec[3];                               // earth centre (eye.x, -R, eye.z)
     float wind_t[3];                           // (wind_dir * wind_speed) * time[1]
     float skew[3];                             // skew_dir
+    // FP64 shell intersections (precision form), per shell (0 inner, 1 outer):
+    // the normalised ray origin (eye - ec) / radius and C = |o|^2 - 1.  Every
+    // ray leaves the eye, so both are the same for the whole frame.
+    double sh_o[2][3];
+    double sh_c[2];
 };
 
 void make_march_frame(Frame* f, const mt_params& p, const mt_camera_ubo& cam, const mt_time_ubo& tm);

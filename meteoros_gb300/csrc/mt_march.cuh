@@ -377,8 +377,9 @@ MT_HD void march_pixel(const MarchArgs& a, const Frame& F, const Tex<S>& tx, int
     const f3 ec = ld3(F.ec);
     Isect in, out;
     if (p.fp64_shells) {
-        in = ray_sphere_fp64(ray.origin, ray.direction, ec, F.Rin);
-        out = ray_sphere_fp64(ray.origin, ray.direction, ec, F.Rout);
+        // ray.origin is the eye: the origin terms are the frame's
+        in = ray_sphere_fp64(F.sh_o[0], F.sh_c[0], ray.direction, ec, F.Rin);
+        out = ray_sphere_fp64(F.sh_o[1], F.sh_c[1], ray.direction, ec, F.Rout);
     } else {
         in = ray_sphere(ray.origin, ray.direction, ec, F.Rin);
         out = ray_sphere(ray.origin, ray.direction, ec, F.Rout);

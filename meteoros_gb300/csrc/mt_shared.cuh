@@ -96,17 +96,17 @@ MT_HD Isect ray_sphere(f3 rO, f3 rD, f3 c, float radius) {
 }
 
 // The same intersection in FP64 (precision form): the normalised-sphere
-// quadratic cancels badly in FP32 (C = |rO|^2 - 1 with |rO| ~ 1).
-MT_HD Isect ray_sphere_fp64(f3 rOf, f3 rDf, f3 cf, float radiusf) {
-    double ox = (double)rOf.x - (double)cf.x, oy = (double)rOf.y - (double)cf.y, oz = (double)rOf.z - (double)cf.z;
+// quadratic cancels badly in FP32 (C = |rO|^2 - 1 with |rO| ~ 1).  The
+// origin terms -- o = (rO - c) / radius and C, the same for every ray of a
+// frame (Frame::sh_o, sh_c) -- come in precomputed: three FP64 divisions and
+// the |o|^2 sum fewer per ray, on a GPU whose FP64 rate is a small fraction
+// of its FP32 rate.
+MT_HD Isect ray_sphere_fp64(const double o[3], double C, f3 rDf, f3 cf, float radiusf) {
+    const double ox = o[0], oy = o[1], oz = o[2];
     const double r = (double)radiusf;
-    ox = ox / r;
-    oy = oy / r;
-    oz = oz / r;
     const double dx = rDf.x, dy = rDf.y, dz = rDf.z;
     double A = dx * dx + dy * dy + dz * dz;
     double B = 2.0 * (dx * ox + dy * oy + dz * oz);
-    double C = (ox * ox + oy * oy + oz * oz) - 1.0;
     double disc = B * B - 4.0 * A * C;
     Isect is;
     is.valid = false;
