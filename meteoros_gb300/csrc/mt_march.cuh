@@ -402,13 +402,19 @@ MT_HD void march_pixel(const MarchArgs& a, const Frame& F, const Tex<S>& tx, int
 // groups_x x groups_y blocks of 4x4 (Renderer.cpp:713-716); each ray is one
 // block's slot pixel.  Full: one ray per pixel.  G consecutive lanes (an
 // aligned segment of a warp) march one ray.  BS threads per CTA (256 by
-// default, 128 or 32 selectable), 64 registers a thread in every case.
+// default, 128 or 32 selectable).  Resident threads per SM: 1024 (64
+// registers a thread) when G lanes share a ray; 1280 (48 registers, a few
+// spills) for one lane per ray, whose full-frame launches run 2-3 % faster
+// for the extra warps while the 4-lane checkerboard launches gain nothing.
 // Every step reads its jitter vector at an index taken from int(t), which
 // differs from lane to lane: from the parameter space a warp's reads at up to
 // 16 different words are served one word at a time, from shared memory in one
 // pass (48 words, 3 apart: distinct banks), so the table is copied there.
+constexpr int march_min_blocks(int G, int BS) {
+    return ((G == 1 ? 1280 : 1024) / BS) < 32 ? ((G == 1 ? 1280 : 1024) / BS) : 32;  // at most 32 CTAs an SM
+}
 template <int G, int S, int BS, bool TR = false>
-__global__ void __launch_bounds__(BS, 1024 / BS) march_kernel(const __grid_constant__ MarchArgs a) {
+__global__ void __launch_bounds__(BS, march_min_blocks(G, BS)) march_kernel(const __grid_constant__ MarchArgs a) {
     static_assert(G >= 1 && G <= 32 && (32 % G) == 0, "G must divide the warp");
     const Frame& F = a.frame;
     const Tex<S> tx = make_tex<S>(a);
