@@ -870,9 +870,14 @@ MT_API mt_status mt_autotune_batch(mt_ctx* ctx, const mt_view* views, int n_view
     if ((st = bind_device(ctx)) != MT_OK) return st;
     const int shapes[4][2] = {{8, 8}, {16, 8}, {16, 16}, {32, 8}};
     const int lane_choices[3] = {1, 4, 8};
-    cudaEvent_t t0, t1;
-    MT_CUDA(ctx, cudaEventCreate(&t0));
-    MT_CUDA(ctx, cudaEventCreate(&t1));
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    cudaError_t e = cudaEventCreate(&t0);
+    if (e == cudaSuccess) e = cudaEventCreate(&t1);
+    if (e != cudaSuccess) {
+        if (t0) cudaEventDestroy(t0);
+        return fail(ctx, MT_ERR_CUDA, "CUDA error %s (%s) creating the autotuner's events", cudaGetErrorName(e),
+                    cudaGetErrorString(e));
+    }
     float best_ms = -1.0f;
     int bw = ctx->batch_tile_w, bh = ctx->batch_tile_h, bl = ctx->batch_lanes, bo = ctx->batch_order;
     st = mt_render_batch(ctx, views, n_views, stream);  // warm-up
@@ -890,8 +895,13 @@ MT_API mt_status mt_autotune_batch(mt_ctx* ctx, const mt_view* views, int n_view
                     cudaEventRecord(t1, (cudaStream_t)stream);
                     if (st != MT_OK) break;
                     float m = 0.0f;
-                    cudaEventSynchronize(t1);
-                    cudaEventElapsedTime(&m, t0, t1);
+                    e = cudaEventSynchronize(t1);
+                    if (e == cudaSuccess) e = cudaEventElapsedTime(&m, t0, t1);
+                    if (e != cudaSuccess) {
+                        st = fail(ctx, MT_ERR_CUDA, "CUDA error %s (%s) timing a tuning candidate", cudaGetErrorName(e),
+                                  cudaGetErrorString(e));
+                        break;
+                    }
                     if (ms < 0.0f || m < ms) ms = m;
                 }
                 if (st == MT_OK && (best_ms < 0.0f || ms < best_ms)) {
