@@ -424,22 +424,20 @@ cudaError_t launch_frame(const MarchArgs& a, cudaStream_t s, const LaunchEvents*
             if (e != cudaSuccess) return e;
             return launch_txaa(t, s, timed ? ev->resolve : nullptr);
         }
-        // on aux the TXAA history taps (launched first: they need only the
-        // previous resolved frame), the raymarch on s, then on aux the
-        // reprojection, which fills the raymarch's last wave; then the TXAA
-        // resolve on s
+        // the raymarch on s, launched first so that its CTAs take the SMs
+        // first; then on aux the TXAA history taps (they need only the
+        // previous resolved frame) and the reprojection, which fill the
+        // raymarch's last waves; then the TXAA resolve on s
         const dim3 block(kTxaaTW, kTxaaTH),
             grid((unsigned)((a.width + kTxaaTW - 1) / kTxaaTW), (unsigned)((a.height + kTxaaTH - 1) / kTxaaTH));
         cudaError_t e = cudaEventRecord(fj->fork, s);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(fj->aux, fj->fork, 0);
-        if (timed) cudaEventRecord(ev->reproject[0], fj->aux);
-        if (e == cudaSuccess) {
-            txaa_history_kernel<<<grid, block, 0, fj->aux>>>(t);
-            e = cudaGetLastError();
-        }
         if (e == cudaSuccess) e = launch_march(a, s, ev);
         if (e != cudaSuccess) return e;
-        e = launch_reproject(a, fj->aux);
+        if (timed) cudaEventRecord(ev->reproject[0], fj->aux);
+        txaa_history_kernel<<<grid, block, 0, fj->aux>>>(t);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = launch_reproject(a, fj->aux);
         if (timed) cudaEventRecord(ev->reproject[1], fj->aux);
         if (e == cudaSuccess) e = cudaEventRecord(fj->join, fj->aux);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(s, fj->join, 0);
