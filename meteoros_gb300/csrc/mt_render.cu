@@ -51,8 +51,9 @@ MT_HD void old_uv(const ViewConsts& v, float sx, float sy, float& old_u, float& 
     const float B = 2.0f * dot3(rD, ro);
     const float disc = B * B - 4.0f * A * v.C;
     if (!(disc < 0.0f)) {
-        float t = (-B - sqrtf(disc)) / (2.0f * A);
-        if (t < 0.0f) t = (-B + sqrtf(disc)) / (2.0f * A);
+        // the first root's sign is its numerator's (2A > 0): one division
+        const float sq = sqrtf(disc), n1 = -B - sq;
+        const float t = (n1 < 0.0f ? -B + sq : n1) / (2.0f * A);
         if (t >= 0.0f) {
             f3 pnt = ro + t * rD;
             pnt = pnt * v.Rin;
@@ -211,19 +212,35 @@ __global__ void __launch_bounds__(256) reproject_kernel(const __grid_constant__ 
 // the nine taps per pixel then read shared memory.
 constexpr int kTxaaTW = 32, kTxaaTH = 8;
 
-// The history taps of a frame, into `out` (which the resolve then reads back
-// and overwrites, pixel by pixel): run beside the raymarch, since they do not
-// depend on the frame being rendered.
-__global__ void __launch_bounds__(kTxaaTW * kTxaaTH) txaa_history_kernel(const __grid_constant__ TxaaArgs a) {
+// The two per-pixel passes of a frame that do not depend on its raymarch, in
+// one kernel run beside it: every pixel's TXAA history tap, into `out`
+// (which the resolve then reads back and overwrites, pixel by pixel), and
+// the reprojection of every pixel the raymarch does not write, into `cur`.
+// One launch instead of two, and each thread has two independent chains.
+__global__ void __launch_bounds__(kTxaaTW * kTxaaTH) history_reproject_kernel(const __grid_constant__ MarchArgs a,
+                                                                              const __grid_constant__ TxaaArgs t) {
+    const int W = a.width, H = a.height;
     const int x = blockIdx.x * kTxaaTW + threadIdx.x, y = blockIdx.y * kTxaaTH + threadIdx.y;
-    if (x >= a.width || y >= a.height) return;
-    const f4v h = txaa_history(a.vc, a.history, x, y, a.width, a.height);
-    a.out[(size_t)y * (size_t)a.width + (size_t)x] = make_float4(h.x, h.y, h.z, h.w);
+    const bool inside = x < W && y < H;
+    const bool reproject = inside && !is_marched(a, x, y);
+    if (inside) {
+        const size_t o = (size_t)y * (size_t)W + (size_t)x;
+        const f4v h = txaa_history(t.vc, t.history, x, y, W, H);
+        if (reproject) {
+            const f4v b = reproject_pixel(a, a.vc_repro, x, y);
+            a.cur[o] = make_float4(b.x, b.y, b.z, b.w);
+        }
+        t.out[o] = make_float4(h.x, h.y, h.z, h.w);
+    }
+    if (a.stats) {
+        Counts none{0u, 0u, 0u};
+        flush_counts(a.stats, none, reproject ? 1u : 0u);
+    }
 }
 
 // The resolve: a 32x8 CTA owns a 32x32 tile, each thread four pixels 8 rows
 // apart (the halo and the barrier are shared by four times the pixels).
-// HISTORY_IN_OUT: the history taps were stored in `out` by txaa_history_kernel.
+// HISTORY_IN_OUT: the history taps were stored in `out` by history_reproject_kernel.
 constexpr int kTxaaRows = 4;
 template <bool HISTORY_IN_OUT>
 __global__ void __launch_bounds__(kTxaaTW * kTxaaTH, 4) txaa_kernel(const __grid_constant__ TxaaArgs a) {
@@ -426,8 +443,8 @@ cudaError_t launch_frame(const MarchArgs& a, cudaStream_t s, const LaunchEvents*
         }
         // the raymarch on s, launched first so that its CTAs take the SMs
         // first; then on aux the TXAA history taps (they need only the
-        // previous resolved frame) and the reprojection, which fill the
-        // raymarch's last waves; then the TXAA resolve on s
+        // previous resolved frame) and the reprojection in one kernel, which
+        // fills the raymarch's last waves; then the TXAA resolve on s
         const dim3 block(kTxaaTW, kTxaaTH),
             grid((unsigned)((a.width + kTxaaTW - 1) / kTxaaTW), (unsigned)((a.height + kTxaaTH - 1) / kTxaaTH));
         cudaError_t e = cudaEventRecord(fj->fork, s);
@@ -435,9 +452,8 @@ cudaError_t launch_frame(const MarchArgs& a, cudaStream_t s, const LaunchEvents*
         if (e == cudaSuccess) e = launch_march(a, s, ev);
         if (e != cudaSuccess) return e;
         if (timed) cudaEventRecord(ev->reproject[0], fj->aux);
-        txaa_history_kernel<<<grid, block, 0, fj->aux>>>(t);
+        history_reproject_kernel<<<grid, block, 0, fj->aux>>>(a, t);
         e = cudaGetLastError();
-        if (e == cudaSuccess) e = launch_reproject(a, fj->aux);
         if (timed) cudaEventRecord(ev->reproject[1], fj->aux);
         if (e == cudaSuccess) e = cudaEventRecord(fj->join, fj->aux);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(s, fj->join, 0);

@@ -82,8 +82,12 @@ MT_HD Isect ray_sphere(f3 rO, f3 rD, f3 c, float radius) {
     float C = dot3(rO, rO) - 1.0f;
     float disc = B * B - 4.0f * A * C;
     if (disc < 0.0f) return is;
-    float t = (-B - sqrtf(disc)) / (2.0f * A);
-    if (t < 0.0f) t = (-B + sqrtf(disc)) / (2.0f * A);
+    // t = (-B - sqrt(disc)) / 2A, or the other root where that is negative.
+    // 2A = 2|rD|^2 > 0, so the first root's sign is its numerator's and only
+    // the root taken is divided (the camera inside the shell always takes the
+    // second).
+    const float sq = sqrtf(disc), n1 = -B - sq;
+    const float t = (n1 < 0.0f ? -B + sq : n1) / (2.0f * A);
     if (t >= 0.0f) {
         f3 pnt = rO + t * rD;
         is.valid = true;
@@ -113,8 +117,8 @@ MT_HD Isect ray_sphere_fp64(const double o[3], double C, f3 rDf, f3 cf, float ra
     is.point = f3{0.0f, 0.0f, 0.0f};
     is.t = 0.0f;
     if (disc < 0.0) return is;
-    double t = (-B - sqrt(disc)) / (2.0 * A);
-    if (t < 0.0) t = (-B + sqrt(disc)) / (2.0 * A);
+    const double sq = sqrt(disc), n1 = -B - sq;  // as in ray_sphere: one division
+    const double t = (n1 < 0.0 ? -B + sq : n1) / (2.0 * A);
     if (t >= 0.0) {
         double px = (ox + t * dx) * r + (double)cf.x;
         double py = (oy + t * dy) * r + (double)cf.y;
