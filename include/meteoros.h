@@ -146,18 +146,19 @@ typedef struct mt_stats {
  * (mt_set_timing).  A kernel that did not run since timing was switched on
  * reads 0. */
 typedef struct mt_kernel_times {
-    float reproject_ms;
-    float march_ms;
-    float txaa_ms;
-    float resolve_ms; /* reprojection fused with TXAA (mt_render_frame) */
+    float reproject_ms; /* the reprojection (mt_render_frame: with the TXAA history taps, one kernel) */
+    float march_ms;     /* the raymarch */
+    float txaa_ms;      /* mt_txaa */
+    float resolve_ms;   /* mt_render_frame's TXAA resolve (fused_resolve: reprojection fused with TXAA) */
 } mt_kernel_times;
 
 /* Launch-shape choices of the kernels.  Results do not depend on them (the
  * tests hold every choice to the same output); only speed does. */
 typedef struct mt_tuning {
     int32_t march_lanes;  /* lanes that march one ray together: 1, 4, 8 or 16; 0 = chosen from the ray count */
-    int32_t fused_resolve; /* mt_render_frame: 0 = reprojection, march, TXAA as three launches (default);
-                            * 1 = march, then reprojection fused with TXAA */
+    int32_t fused_resolve; /* mt_render_frame: 0 = the raymarch, the TXAA history taps and the
+                            * reprojection in one kernel beside it, then the TXAA resolve (default);
+                            * 1 = the raymarch, then the reprojection fused with the TXAA resolve */
     int32_t batch_tile_w;  /* mt_render_batch: tile of rays a CTA takes at a time (default 16 x 8) */
     int32_t batch_tile_h;
     int32_t batch_lanes;   /* mt_render_batch: lanes per ray, 1, 4, 8 or 16 (default 1) */
