@@ -671,6 +671,8 @@ def run_gb300(args) -> int:
         "roofline": {"bound": "hbm", "kernel": "march_kernel", "achieved": round(achieved, 2),
                      "peak": hbm_peak, "unit": "GB/s", "frac": round(achieved / hbm_peak, 5),
                      "traffic": MARCH_DRAM_BYTES_PER_LAUNCH, "algorithmic_bytes": march_bytes,
+                     "launch_ms": round(march_ms, 5), "launch_timing": "the raymarch's launch timed alone "
+                     "(the frames again with the reprojection serialised before it), CUDA events on its stream",
                      "peak_source": peak_src,
                      "note": "the raymarch is FP32-issue and texel-latency bound, not HBM bound: its algorithmic HBM "
                              "bytes are the colour and mask writes plus one read of the 9.5 MB of RGBA8 volumes; "
@@ -679,7 +681,7 @@ def run_gb300(args) -> int:
         "roofline_fp32": {"bound": "fp32", "kernel": "march_kernel",
                           "achieved": round(march_flops / (march_ms * 1e-3) / 1e12, 3), "peak": round(fp32_peak, 2),
                           "unit": "TFLOP/s", "frac": round(march_flops / (march_ms * 1e-3) / 1e12 / fp32_peak, 4),
-                          "flops_per_launch": int(march_flops),
+                          "flops_per_launch": int(march_flops), "launch_ms": round(march_ms, 5),
                           "peak_source": "nominal: SMs x 128 FP32 lanes x max SM clock, one non-fused op per lane "
                                          "per clock (the kernels are built without contraction)"},
         # filtered texel fetches of the raymarch from the exact counters: per primary
