@@ -403,6 +403,34 @@ def test_fused_frame_equals_render_then_txaa(ctx, size):
         ctx.set_tuning(fused_resolve=False, reproject_serial=False)
 
 
+@pytest.mark.parametrize("size", [(33, 9), (641, 361)])
+def test_frame_counters_equal_render(ctx, size):
+    """The executed-sample and pixel counters of mt_render_frame (the
+    reprojection counted inside the history-taps + reprojection kernel, or the
+    reprojection kernel when serialised) equal mt_render's for the same frame."""
+    w, h = size
+    cam_old, tm, params, (yaw, pitch) = scenes.config_view(9, w, h)
+    cam = scenes.look((0.0, 100.0, 0.0), yaw + 0.5, pitch, 60.0, w, h)
+    rng = np.random.default_rng(w * h)
+    prev = to_dev(rng.random((h, w, 4), dtype=np.float32), torch)
+    hist = to_dev(rng.random((h, w, 4), dtype=np.float32), torch)
+    flags = abi.MT_RENDER_CHECKERBOARD | abi.MT_RENDER_COUNT
+    tm.frame_count_mod16 = 6
+    cur = torch.zeros((h, w, 4), dtype=torch.float32, device="cuda")
+    out = torch.zeros_like(cur)
+    ctx.stats(reset=True)
+    ctx.render(cam, cam_old, tm, params, prev, cur, None, flags)
+    ref = ctx.stats(reset=True)
+    want = (ref.primary_samples, ref.light_samples, ref.marched_rays, ref.pixels)
+    assert ref.pixels == w * h
+    for serial in (False, True):
+        ctx.set_tuning(reproject_serial=serial)
+        ctx.render_frame(cam, cam_old, tm, params, prev, cur, hist, out, None, flags)
+        st = ctx.stats(reset=True)
+        assert (st.primary_samples, st.light_samples, st.marched_rays, st.pixels) == want, serial
+    ctx.set_tuning(reproject_serial=False)
+
+
 def test_config1_chain_16_frames(ctx, oracle, vol7):
     """A 16-frame config-1 sequence at 480x270 through Session (the
     reference's ping-pong, Renderer.cpp:131-136, 191): each frame reprojects
