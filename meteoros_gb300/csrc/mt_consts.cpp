@@ -1,10 +1,13 @@
-// Per-frame constants of the reprojection / TXAA geometry (ViewConsts in
-// mt_kernels.h), computed on the host once per launch.  Every value is the
-// IEEE FP32 result of the same operations, in the same order, that the
-// per-pixel code performs (cast_ray, jitter_offset and ray_sphere of
-// mt_shared.cuh), so the kernels give the same bits as when each pixel
-// computed them.  Built with -ffp-contract=off: no fused multiply-add may
-// change a rounding.
+// Per-frame constants, computed on the host once per launch: the
+// reprojection / TXAA geometry (ViewConsts in mt_kernels.h) and the
+// raymarch's frame terms (Frame: shell radii and reciprocals, wind and skew,
+// the per-step jitter, the sun direction and cone-light kernel of
+// ray_consts, the FP64 shell intersections' origin terms).  Every value is
+// the IEEE result of the same operations, in the same order, that the
+// per-pixel code performed (cast_ray, jitter_offset, ray_sphere,
+// ray_sphere_fp64, ray_consts), so the kernels give the same bits as when
+// each pixel or ray computed them.  Built with -ffp-contract=off: no fused
+// multiply-add may change a rounding.
 #include <cmath>
 #include <cuda_runtime.h>
 
@@ -100,6 +103,33 @@ void make_march_frame(Frame* f, const mt_params& p, const mt_camera_ubo& cam, co
     f->ec[0] = f->eye[0];
     f->ec[1] = -f->R;
     f->ec[2] = f->eye[2];
+    // ray_consts' sun direction and cone-light kernel, in its order of operations
+    float ld[3];
+    normalize(ld, p.sun_light_pos[0] - f->eye[0], p.sun_light_pos[1] - f->eye[1], p.sun_light_pos[2] - f->eye[2]);
+    for (int i = 0; i < 3; ++i) f->light_dir[i] = ld[i];
+    {
+        const float ax = std::fabs(ld[0]), ay = std::fabs(ld[1]), az = std::fabs(ld[2]);
+        float mc[3] = {0.0f, 0.0f, 0.0f};
+        if (ax > ay && ax > az)
+            mc[0] = ax;
+        else if (ay > ax && ay > az)
+            mc[1] = ay;
+        else
+            mc[2] = az;
+        auto cross = [](float o[3], const float a[3], const float b[3]) {
+            o[0] = a[1] * b[2] - b[1] * a[2];
+            o[1] = a[2] * b[0] - b[2] * a[0];
+            o[2] = a[0] * b[1] - b[0] * a[1];
+        };
+        float zc[3], xc[3];
+        cross(zc, ld, mc);
+        cross(xc, zc, ld);
+        static const float k[6][3] = {{0.1f, 0.25f, -0.15f}, {0.2f, 0.5f, 0.2f},   {-0.2f, 0.1f, -0.1f},
+                                      {-0.05f, 0.75f, 0.05f}, {-0.1f, 1.0f, 0.0f}, {0.0f, 3.0f, 0.0f}};
+        for (int i = 0; i < 6; ++i)
+            for (int c = 0; c < 3; ++c)  // mat3(xC, lightDir, zC) * k[i]
+                f->cone[i][c] = xc[c] * k[i][0] + ld[c] * k[i][1] + zc[c] * k[i][2];
+    }
     // ray_sphere_fp64's origin terms, in its order of operations
     const float radii[2] = {f->Rin, f->Rout};
     for (int s = 0; s < 2; ++s) {

@@ -48,6 +48,10 @@ struct Frame {
     // ray leaves the eye, so both are the same for the whole frame.
     double sh_o[2][3];
     double sh_c[2];
+    // The sun direction normalize(sun - eye) and the six cone-light kernel
+    // vectors of cloudRayMarch.comp:598-624, the same for every ray
+    float light_dir[3];
+    float cone[6][3];
 };
 
 void make_march_frame(Frame* f, const mt_params& p, const mt_camera_ubo& cam, const mt_time_ubo& tm);

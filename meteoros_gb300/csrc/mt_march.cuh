@@ -161,30 +161,15 @@ MT_HD void ray_consts(const mt_params& p, const Frame& F, f3 dir, f3 startPos, f
     rc.dir = dir;
     rc.startPos = startPos;
     rc.stepSize = stepSize;
-    const f3 lightDir = normalize3(ld3(p.sun_light_pos) - ld3(F.eye));
+    // the sun direction and the cone-light kernel are the frame's (Frame::light_dir, cone)
+    const f3 lightDir = ld3(F.light_dir);
     rc.cos_angle = dot3(normalize3(dir), lightDir);
     rc.cos_q = (rc.cos_angle - 0.7f) / (1.0f - 0.7f);
     rc.HG_light = gmax(henyey_greenstein(rc.cos_angle, 0.6f), 0.7f * henyey_greenstein(rc.cos_angle, 0.99f - 0.1f));
-    float ax = fabsf(lightDir.x), ay = fabsf(lightDir.y), az = fabsf(lightDir.z);
-    f3 maxComp;
-    if (ax > ay && ax > az)
-        maxComp = f3{ax, 0.0f, 0.0f};
-    else if (ay > ax && ay > az)
-        maxComp = f3{0.0f, ay, 0.0f};
-    else
-        maxComp = f3{0.0f, 0.0f, az};
-    f3 zC = cross3(lightDir, maxComp);
-    f3 xC = cross3(zC, lightDir);
-    const f3 kernel[6] = {mat3mul(xC, lightDir, zC, f3{0.1f, 0.25f, -0.15f}),
-                          mat3mul(xC, lightDir, zC, f3{0.2f, 0.5f, 0.2f}),
-                          mat3mul(xC, lightDir, zC, f3{-0.2f, 0.1f, -0.1f}),
-                          mat3mul(xC, lightDir, zC, f3{-0.05f, 0.75f, 0.05f}),
-                          mat3mul(xC, lightDir, zC, f3{-0.1f, 1.0f, 0.0f}),
-                          mat3mul(xC, lightDir, zC, f3{0.0f, 3.0f, 0.0f})};
     // the step-independent part of the light sample position
     // pos + ((stepSize * kernel[i]) * i) (cloudRayMarch.comp:656)
     // in units of the layer thickness, as the light samples' positions are used
-    for (int i = 0; i < 6; ++i) rc.koff[i] = ((stepSize * kernel[i]) * (float)i) * F.r_thick.y;
+    for (int i = 0; i < 6; ++i) rc.koff[i] = ((stepSize * ld3(F.cone[i])) * (float)i) * F.r_thick.y;
     rc.lenInner = length3(startPos - ld3(F.eye));
 }
 
