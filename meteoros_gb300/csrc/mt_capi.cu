@@ -1053,7 +1053,7 @@ static_assert(sizeof(mt::MarchArgs) % 4 == 0, "view tables are stored as 32-bit 
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
 
-// Views per store launch: 16 view tables (~25 KB) stay inside the 32 KB of
+// Views per store launch: 16 view tables (~26 KB) stay inside the 32 KB of
 // kernel parameter space.
 constexpr int kNoallocStoreViews = 16;
 constexpr int kViewWords = (int)(sizeof(mt::MarchArgs) / 4);
