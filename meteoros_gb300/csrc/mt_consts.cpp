@@ -1,13 +1,17 @@
-// Per-frame constants, computed on the host once per launch: the
-// reprojection / TXAA geometry (ViewConsts in mt_kernels.h) and the
+// Per-frame constants, computed on the host once per launch: the camera
+// geometry of castRay / reprojection / TXAA (ViewConsts in mt_kernels.h:
+// camera basis, slot jitter, ref, the inner shell's origin terms) and the
 // raymarch's frame terms (Frame: shell radii and reciprocals, wind and skew,
 // the per-step jitter, the sun direction and cone-light kernel of
-// ray_consts, the FP64 shell intersections' origin terms).  Every value is
-// the IEEE result of the same operations, in the same order, that the
-// per-pixel code performed (cast_ray, jitter_offset, ray_sphere,
-// ray_sphere_fp64, ray_consts), so the kernels give the same bits as when
-// each pixel or ray computed them.  Built with -ffp-contract=off: no fused
-// multiply-add may change a rounding.
+// ray_consts, the sky's sun terms, the FP64 shell intersections' origin
+// terms).  Each value is the result of the same operations, in the same
+// order, that the shaders perform per pixel or per ray (cloudRayMarch.comp
+// castRay / getJitterOffset :114-226, raySphereIntersection :229-273, the
+// cone set-up :598-624, the sky :401-467), so the kernels give the bits they
+// gave when each pixel or ray computed them -- the IEEE operations exactly;
+// the sky's acos / pow / exp are the host's, within a few ulp of the
+// device's.  Built with -ffp-contract=off: no fused multiply-add may change
+// a rounding.
 #include <cmath>
 #include <cuda_runtime.h>
 
@@ -129,6 +133,31 @@ void make_march_frame(Frame* f, const mt_params& p, const mt_camera_ubo& cam, co
         for (int i = 0; i < 6; ++i)
             for (int c = 0; c < 3; ++c)  // mat3(xC, lightDir, zC) * k[i]
                 f->cone[i][c] = xc[c] * k[i][0] + ld[c] * k[i][1] + zc[c] * k[i][2];
+    }
+    // atmosphere_color's sun terms, in its order of operations
+    {
+        float sd[3], ss[3];
+        normalize(sd, p.sky_sun_pos[0] - f->eye[0], p.sky_sun_pos[1] - f->eye[1], p.sky_sun_pos[2] - f->eye[2]);
+        normalize(ss, p.sky_sun_pos[0], p.sky_sun_pos[1], p.sky_sun_pos[2]);
+        auto gmin_ = [](float a, float b) { return b < a ? b : a; };
+        auto gmax_ = [](float a, float b) { return a < b ? b : a; };
+        const float zc = gmin_(gmax_(ss[1], -1.0f), 1.0f);
+        const float sunI =
+            1000.0f * gmax_(0.0f, 1.0f - std::pow(2.718281828459f, -((1.6110731557f - std::acos(zc)) / 1.5f)));
+        const float sunFade = 1.0f - gmin_(gmax_(1.0f - std::exp(p.sky_sun_pos[1] / 450000.0f), 0.0f), 1.0f);
+        static const float RT[3] = {5.804542996261093E-6f, 1.3562911419845635E-5f, 3.0265902468824876E-5f};
+        static const float MIE[3] = {1.839991851443397f, 2.779802391966052f, 4.079047954386109f};
+        const float rs = 2.0f - 1.0f + sunFade;
+        const float c = (0.2f * 10.0f) * 10E-18f;
+        for (int i = 0; i < 3; ++i) {
+            f->sky_sun_dir[i] = sd[i];
+            f->sky_betaR[i] = RT[i] * rs;
+            f->sky_betaM[i] = ((0.434f * c) * MIE[i]) * 0.005f;
+            f->sky_betaRM[i] = f->sky_betaR[i] + f->sky_betaM[i];
+        }
+        f->sky_sunE = 0.780f * sunI;
+        float yd = 1.0f - sd[1];
+        f->sky_yDot = yd * (yd * yd * yd * yd);
     }
     // ray_sphere_fp64's origin terms, in its order of operations
     const float radii[2] = {f->Rin, f->Rout};

@@ -52,6 +52,10 @@ struct Frame {
     // vectors of cloudRayMarch.comp:598-624, the same for every ray
     float light_dir[3];
     float cone[6][3];
+    // atmosphere_color's terms that depend on the sun only (cloudRayMarch.comp:401-467)
+    float sky_sun_dir[3];  // normalize(sky_sun_pos - eye)
+    float sky_sunE, sky_yDot;
+    float sky_betaR[3], sky_betaM[3], sky_betaRM[3];
 };
 
 void make_march_frame(Frame* f, const mt_params& p, const mt_camera_ubo& cam, const mt_time_ubo& tm);

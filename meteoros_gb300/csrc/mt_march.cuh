@@ -327,12 +327,13 @@ template <int G, int S, bool TR = false>
 MT_HD void march_pixel(const MarchArgs& a, const Frame& F, const Tex<S>& tx, int px, int py, Counts& cnt,
                        unsigned gmask, int lane, const float (*jitter)[3]) {
     const mt_params& p = a.params;
-    const int W = a.width, H = a.height;
-    const int pixelID = a.time.frame_count_mod16;
-    float ux = (float)px / (float)W, uy = (float)py / (float)H;
+    const int W = a.width;
+    // this frame's camera basis and cloudRayMarch.comp's jitter: the TXAA
+    // geometry constants (the same camera, slot and image size)
+    const ViewConsts& vc = a.vc_txaa;
+    float ux = rdiv((float)px, Rcp{vc.r_w[0], vc.r_w[1]}), uy = rdiv((float)py, Rcp{vc.r_h[0], vc.r_h[1]});
     uy = 1.0f - uy;
-    Ray ray = cast_ray(ux, uy, ld3(F.eye), a.camera, a.time, pixelID, W, H, false);
-    const float sunIntensity = 0.780f;
+    const Ray ray = cast_ray(vc, ld3(F.eye), ux, uy);
     float _dot = dot3(f3{0.0f, 1.0f, 0.0f}, ray.direction);
     const float bgMul = gmax(0.620f, _dot);
     const float fade = 0.06f;
@@ -349,7 +350,7 @@ MT_HD void march_pixel(const MarchArgs& a, const Frame& F, const Tex<S>& tx, int
         }
         return;
     }
-    bg = atmosphere_color(p, ray.direction, ld3(p.sky_sun_pos) - ray.origin, sunIntensity);
+    bg = atmosphere_color(F, ray.direction);  // sunIntensity 0.780 is in F.sky_sunE
     bg = bg * bgMul;
     if (_dot < fade) {
         if (lane == 0) {

@@ -38,13 +38,7 @@ MT_HD bool is_marched(const MarchArgs& a, int x, int y) {
 MT_HD Rcp rcp_of(const float r[2]) { return Rcp{r[0], r[1]}; }
 
 MT_HD void old_uv(const ViewConsts& v, float sx, float sy, float& old_u, float& old_v) {
-    float nx = sx * 2.0f - 1.0f, ny = sy * 2.0f - 1.0f;
-    nx = nx + v.jx;
-    ny = ny + v.jy;
-    const f3 cam_x = (nx * v.tanx) * ld3(v.right);
-    const f3 cam_y = (ny * v.tany) * ld3(v.up);
-    const f3 pp = ld3(v.ref) + cam_x + cam_y;
-    const f3 rD = normalize3_r(pp - ld3(v.eye));
+    const f3 rD = cast_ray(v, ld3(v.eye), sx, sy).direction;
     const f3 ro = ld3(v.ro);
     f3 q{0.0f, 0.0f, 0.0f};
     const float A = dot3(rD, rD);

@@ -26,46 +26,19 @@ struct Isect {
     float t;
 };
 
-// cloudRayMarch.comp:114-132; reprojection.comp:72-90 reads halton 1/2 again
-// for index >= 4 (`repro`).
-MT_HD void jitter_offset(const mt_time_ubo& tm, int index, float dimx, float dimy, bool repro, float& jx,
-                         float& jy) {
-    index = index / 2;
-    float x, y;
-    if (index < 4) {
-        x = tm.halton_seq1[index];
-        y = tm.halton_seq2[index];
-    } else {
-        index -= 4;
-        if (repro) {
-            x = tm.halton_seq1[index];
-            y = tm.halton_seq2[index];
-        } else {
-            x = tm.halton_seq3[index];
-            y = tm.halton_seq4[index];
-        }
-    }
-    jx = x / dimx;
-    jy = y / dimy;
-}
-
-// cloudRayMarch.comp:194-226
-MT_HD Ray cast_ray(float sx, float sy, f3 eye, const mt_camera_ubo& cam, const mt_time_ubo& tm, int pixelID, int W,
-                   int H, bool repro) {
-    const float* v = cam.view;
-    f3 camRight = normalize3(f3{v[0], v[4], v[8]});
-    f3 camUp = normalize3(f3{v[1], v[5], v[9]});
-    f3 camLook = -normalize3(f3{v[2], v[6], v[10]});
+// cloudRayMarch.comp:194-226 (castRay, with getJitterOffset :114-132) for
+// screen point (sx, sy).  The camera basis, the jitter of this frame's slot
+// and ref = eye + look are the same for every pixel: they come in `v`, made
+// on the host by make_view_consts with the same operations (mt_consts.cpp),
+// and each ray computes only its own part.
+MT_HD Ray cast_ray(const ViewConsts& v, f3 eye, float sx, float sy) {
     float nx = sx * 2.0f - 1.0f, ny = sy * 2.0f - 1.0f;
-    float jx, jy;
-    jitter_offset(tm, pixelID, (float)W, (float)H, repro, jx, jy);
-    nx = nx + jx;
-    ny = ny + jy;
-    f3 cam_x = (nx * cam.tan_fov_by_2[0]) * camRight;
-    f3 cam_y = (ny * cam.tan_fov_by_2[1]) * camUp;
-    f3 ref = eye + camLook;
-    f3 pp = ref + cam_x + cam_y;
-    return Ray{eye, normalize3(pp - eye)};
+    nx = nx + v.jx;
+    ny = ny + v.jy;
+    const f3 cam_x = (nx * v.tanx) * ld3(v.right);
+    const f3 cam_y = (ny * v.tany) * ld3(v.up);
+    const f3 pp = ld3(v.ref) + cam_x + cam_y;
+    return Ray{eye, normalize3_r(pp - eye)};
 }
 
 // cloudRayMarch.comp:229-273 (t = length(p - rO) with the normalised rO, as
@@ -217,21 +190,16 @@ MT_HD float light_energy(float h, float dl, float ds, float phase, float cos_q, 
     return att * primary * in_scatter * phase * brightness;
 }
 
-// cloudRayMarch.comp:401-467 (Preetham).  Once per ray: kept out of line so
-// the march loop stays small in the instruction cache.
-static __device__ __noinline__ f3 atmosphere_color(const mt_params& p, f3 dir, f3 sunDir, float sunIntensity) {
-    const f3 skySun = ld3(p.sky_sun_pos);
+// cloudRayMarch.comp:401-467 (Preetham) for ray direction `dir`.  The terms
+// that depend on the sun only -- its direction from the eye, sunE, the
+// Rayleigh and Mie coefficients and yDot -- are the frame's (Frame::sky_*,
+// made on the host by make_march_frame with the same operations); the rest
+// is per ray.  Once per ray: kept out of line so the march loop stays small
+// in the instruction cache.
+static __device__ __noinline__ f3 atmosphere_color(const Frame& F, f3 dir) {
     const float PI = 3.14159265f;
-    sunDir = normalize3(sunDir);
-    float zenithAngleCos = gclamp(normalize3(skySun).y, -1.0f, 1.0f);
-    float sunI = 1000.0f * gmax(0.0f, 1.0f - powf(2.718281828459f, -((1.6110731557f - acosf(zenithAngleCos)) / 1.5f)));
-    float sunE = sunIntensity * sunI;
-    float sunFade = 1.0f - gclamp(1.0f - expf(skySun.y / 450000.0f), 0.0f, 1.0f);
-    const f3 RT{5.804542996261093E-6f, 1.3562911419845635E-5f, 3.0265902468824876E-5f};
-    f3 BetaR = RT * (2.0f - 1.0f + sunFade);
-    float c = (0.2f * 10.0f) * 10E-18f;
-    const f3 MIE{1.839991851443397f, 2.779802391966052f, 4.079047954386109f};
-    f3 BetaM = ((0.434f * c) * MIE) * 0.005f;
+    const f3 sunDir = ld3(F.sky_sun_dir), BetaR = ld3(F.sky_betaR), BetaM = ld3(F.sky_betaM);
+    const float sunE = F.sky_sunE;
     float zenith = acosf(gmax(0.0f, dir.y));
     float inverse = 1.0f / (cosf(zenith) + 0.15f * powf(93.885f - ((zenith * 180.0f) / PI), -1.253f));
     float sR = 8.4E3f * inverse;
@@ -244,14 +212,12 @@ static __device__ __noinline__ f3 atmosphere_color(const mt_params& p, f3 dir, f
     f3 betaRTheta = BetaR * rPhase;
     float mPhase = henyey_greenstein(cosTheta, 0.8f);
     f3 betaMTheta = BetaM * mPhase;
-    float yDot = 1.0f - sunDir.y;
-    yDot = yDot * (yDot * yDot * yDot * yDot);
-    f3 betas = (betaRTheta + betaMTheta) / (BetaR + BetaM);
+    f3 betas = (betaRTheta + betaMTheta) / ld3(F.sky_betaRM);
     f3 a = (sunE * betas) * (f3{1.0f, 1.0f, 1.0f} - fex);
     f3 Lin{powf(a.x, 1.5f), powf(a.y, 1.5f), powf(a.z, 1.5f)};
     f3 b = (sunE * betas) * fex;
     f3 pb{powf(b.x, 0.5f), powf(b.y, 0.5f), powf(b.z, 0.5f)};
-    Lin = Lin * mix3(f3{1.0f, 1.0f, 1.0f}, pb, gclamp(yDot, 0.0f, 1.0f));
+    Lin = Lin * mix3(f3{1.0f, 1.0f, 1.0f}, pb, gclamp(F.sky_yDot, 0.0f, 1.0f));
     f3 L0 = 0.1f * fex;
     const float SAC = 0.999956676946448443553574619906976478926848692873900859324f;
     float sunDisk = gsmoothstep(SAC, SAC + 0.00002f, cosTheta);
