@@ -159,8 +159,13 @@ void make_march_frame(Frame* f, const mt_params& p, const mt_camera_ubo& cam, co
         float yd = 1.0f - sd[1];
         f->sky_yDot = yd * (yd * yd * yd * yd);
     }
-    // ray_sphere_fp64's origin terms, in its order of operations
+    // ray_sphere's and ray_sphere_fp64's origin terms, in their orders of operations
     const float radii[2] = {f->Rin, f->Rout};
+    for (int s = 0; s < 2; ++s) {
+        for (int i = 0; i < 3; ++i) f->sh32_o[s][i] = (f->eye[i] - f->ec[i]) / radii[s];
+        const float* o = f->sh32_o[s];
+        f->sh32_c[s] = (o[0] * o[0] + o[1] * o[1] + o[2] * o[2]) - 1.0f;
+    }
     for (int s = 0; s < 2; ++s) {
         const double r = (double)radii[s];
         for (int i = 0; i < 3; ++i) f->sh_o[s][i] = ((double)f->eye[i] - (double)f->ec[i]) / r;

@@ -48,6 +48,9 @@ struct Frame {
     // ray leaves the eye, so both are the same for the whole frame.
     double sh_o[2][3];
     double sh_c[2];
+    // The same terms in FP32 for ray_sphere (the plain form)
+    float sh32_o[2][3];
+    float sh32_c[2];
     // The sun direction normalize(sun - eye) and the six cone-light kernel
     // vectors of cloudRayMarch.comp:598-624, the same for every ray
     float light_dir[3];

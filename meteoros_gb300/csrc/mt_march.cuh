@@ -163,8 +163,8 @@ MT_HD void ray_consts(const mt_params& p, const Frame& F, f3 dir, f3 startPos, f
     rc.stepSize = stepSize;
     // the sun direction and the cone-light kernel are the frame's (Frame::light_dir, cone)
     const f3 lightDir = ld3(F.light_dir);
-    rc.cos_angle = dot3(normalize3(dir), lightDir);
-    rc.cos_q = (rc.cos_angle - 0.7f) / (1.0f - 0.7f);
+    rc.cos_angle = dot3(normalize3_r(dir), lightDir);
+    rc.cos_q = rdiv(rc.cos_angle - 0.7f, MT_RCP(0.7f, 1.0f));
     rc.HG_light = gmax(henyey_greenstein(rc.cos_angle, 0.6f), 0.7f * henyey_greenstein(rc.cos_angle, 0.99f - 0.1f));
     // the step-independent part of the light sample position
     // pos + ((stepSize * kernel[i]) * i) (cloudRayMarch.comp:656)
@@ -367,8 +367,8 @@ MT_HD void march_pixel(const MarchArgs& a, const Frame& F, const Tex<S>& tx, int
         in = ray_sphere_fp64(F.sh_o[0], F.sh_c[0], ray.direction, ec, F.Rin);
         out = ray_sphere_fp64(F.sh_o[1], F.sh_c[1], ray.direction, ec, F.Rout);
     } else {
-        in = ray_sphere(ray.origin, ray.direction, ec, F.Rin);
-        out = ray_sphere(ray.origin, ray.direction, ec, F.Rout);
+        in = ray_sphere(F.sh32_o[0], F.sh32_c[0], ray.direction, ec, F.Rin);
+        out = ray_sphere(F.sh32_o[1], F.sh32_c[1], ray.direction, ec, F.Rout);
     }
     float accum = 0.0f;
     if (TR) cnt.sig = 2166136261u;

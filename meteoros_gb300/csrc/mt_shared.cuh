@@ -43,16 +43,17 @@ MT_HD Ray cast_ray(const ViewConsts& v, f3 eye, float sx, float sy) {
 
 // cloudRayMarch.comp:229-273 (t = length(p - rO) with the normalised rO, as
 // the reference defines it).
-MT_HD Isect ray_sphere(f3 rO, f3 rD, f3 c, float radius) {
+// The origin terms rO = (eye - c) / radius and C = dot(rO, rO) - 1 are the
+// same for every ray of a frame (every ray leaves the eye): they come in
+// precomputed (Frame::sh32_o, sh32_c).
+MT_HD Isect ray_sphere(const float o[3], float C, f3 rD, f3 c, float radius) {
     Isect is;
     is.valid = false;
     is.point = f3{0.0f, 0.0f, 0.0f};
     is.t = 0.0f;
-    rO = rO - c;
-    rO = rO / radius;
+    const f3 rO = ld3(o);
     float A = dot3(rD, rD);
     float B = 2.0f * dot3(rD, rO);
-    float C = dot3(rO, rO) - 1.0f;
     float disc = B * B - 4.0f * A * C;
     if (disc < 0.0f) return is;
     // t = (-B - sqrt(disc)) / 2A, or the other root where that is negative.
