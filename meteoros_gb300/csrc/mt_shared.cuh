@@ -168,10 +168,12 @@ MT_HD Erosion make_erosion(float modifier) {
 }
 MT_HD float erode(float baseCloud, const Erosion& e) { return 0.0f + (((baseCloud - e.lo) / e.r.b) * (1.0f - 0.0f)); }
 
-// cloudRayMarch.comp:295-306
+// cloudRayMarch.comp:295-306.  The phase weights the light energy and the
+// sky, colour only: pow in the special-function unit's form (see
+// light_energy).
 MT_HD float henyey_greenstein(float c, float e) {
     float num = 1.0f - e * e;
-    float den = powf((1.0f + e * e - 2.0f * e * c), 1.5f);
+    float den = __powf((1.0f + e * e - 2.0f * e * c), 1.5f);
     return (num / den) * 0.07957747154594767f;
 }
 
@@ -195,18 +197,19 @@ MT_HD float light_energy(float h, float dl, float ds, float phase, float cos_q, 
 // that depend on the sun only -- its direction from the eye, sunE, the
 // Rayleigh and Mie coefficients and yDot -- are the frame's (Frame::sky_*,
 // made on the host by make_march_frame with the same operations); the rest
-// is per ray.  Once per ray: kept out of line so the march loop stays small
-// in the instruction cache.
+// is per ray, its exp and pow in the special-function unit's forms as in
+// light_energy (the background reaches colour only).  Once per ray: kept out
+// of line so the march loop stays small in the instruction cache.
 static __device__ __noinline__ f3 atmosphere_color(const Frame& F, f3 dir) {
     const float PI = 3.14159265f;
     const f3 sunDir = ld3(F.sky_sun_dir), BetaR = ld3(F.sky_betaR), BetaM = ld3(F.sky_betaM);
     const float sunE = F.sky_sunE;
     float zenith = acosf(gmax(0.0f, dir.y));
-    float inverse = 1.0f / (cosf(zenith) + 0.15f * powf(93.885f - ((zenith * 180.0f) / PI), -1.253f));
+    float inverse = 1.0f / (cosf(zenith) + 0.15f * __powf(93.885f - ((zenith * 180.0f) / PI), -1.253f));
     float sR = 8.4E3f * inverse;
     float sM = 1.25E3f * inverse;
     f3 ex = (-BetaR) * sR + BetaM * sM;
-    f3 fex{expf(ex.x), expf(ex.y), expf(ex.z)};
+    f3 fex{__expf(ex.x), __expf(ex.y), __expf(ex.z)};
     float cosTheta = dot3(sunDir, dir);
     float rp = cosTheta * 0.5f + 0.5f;
     float rPhase = 0.05968310365946075f * (1.0f + rp * rp);
@@ -215,9 +218,9 @@ static __device__ __noinline__ f3 atmosphere_color(const Frame& F, f3 dir) {
     f3 betaMTheta = BetaM * mPhase;
     f3 betas = (betaRTheta + betaMTheta) / ld3(F.sky_betaRM);
     f3 a = (sunE * betas) * (f3{1.0f, 1.0f, 1.0f} - fex);
-    f3 Lin{powf(a.x, 1.5f), powf(a.y, 1.5f), powf(a.z, 1.5f)};
+    f3 Lin{__powf(a.x, 1.5f), __powf(a.y, 1.5f), __powf(a.z, 1.5f)};
     f3 b = (sunE * betas) * fex;
-    f3 pb{powf(b.x, 0.5f), powf(b.y, 0.5f), powf(b.z, 0.5f)};
+    f3 pb{__powf(b.x, 0.5f), __powf(b.y, 0.5f), __powf(b.z, 0.5f)};
     Lin = Lin * mix3(f3{1.0f, 1.0f, 1.0f}, pb, gclamp(F.sky_yDot, 0.0f, 1.0f));
     f3 L0 = 0.1f * fex;
     const float SAC = 0.999956676946448443553574619906976478926848692873900859324f;
