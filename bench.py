@@ -59,7 +59,7 @@ FLOPS_PER_PIXEL, FLOPS_PER_RAY, FLOPS_PER_PRIMARY, FLOPS_PER_LIGHT = 132.6, 506.
 # volumes in the samplers' layout (plane quads of the base and detail
 # volumes, bilinear cells of the curl and weather maps, ~37 MB) and the part
 # of the colour and mask writes that leaves L2 during the launch.
-MARCH_DRAM_BYTES_PER_LAUNCH = 34119424 + 1912576
+MARCH_DRAM_BYTES_PER_LAUNCH = 34007296 + 1409792
 
 
 def parse():
