@@ -123,17 +123,10 @@ MT_HD float length3(f3 a) { return sqrtf(dot3(a, a)); }
 MT_HD f3 normalize3(f3 a) { return a / length3(a); }
 // normalize(v) = v / length(v), the three divisions sharing one reciprocal.
 MT_HD f3 normalize3_r(f3 a) { return rdiv3(a, make_rcp(length3(a))); }
-MT_HD f3 cross3(f3 a, f3 b) { return f3{a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y}; }
 MT_HD f3 mix3(f3 x, f3 y, float a) { return f3{gmix(x.x, y.x, a), gmix(x.y, y.y, a), gmix(x.z, y.z, a)}; }
 MT_HD f4v min4(f4v a, f4v b) { return f4v{gmin(a.x, b.x), gmin(a.y, b.y), gmin(a.z, b.z), gmin(a.w, b.w)}; }
 MT_HD f4v max4(f4v a, f4v b) { return f4v{gmax(a.x, b.x), gmax(a.y, b.y), gmax(a.z, b.z), gmax(a.w, b.w)}; }
 MT_HD f3 ld3(const float* p) { return f3{p[0], p[1], p[2]}; }
-
-// GLSL mat3(c0,c1,c2) * v
-MT_HD f3 mat3mul(f3 c0, f3 c1, f3 c2, f3 v) {
-    return f3{c0.x * v.x + c1.x * v.y + c2.x * v.z, c0.y * v.x + c1.y * v.y + c2.y * v.z,
-              c0.z * v.x + c1.z * v.y + c2.z * v.z};
-}
 
 MT_HD float lerp1(float p, float q, float t) { return p + t * (q - p); }
 
