@@ -336,7 +336,7 @@ MT_API mt_status mt_autotune_batch(mt_ctx* ctx, const mt_view* views, int n_view
  * path: cudaMalloc and cudaFree synchronise the device and stall every other
  * stream of a frame loop, and a host that has handed its HBM budget to its
  * own pool has none left to give.  The view table, tile list and work
- * counter live in one fixed device array of the library (about 0.7 MB):
+ * counter live in one fixed device array of the library (about 0.76 MB):
  * at most MT_NOALLOC_MAX_VIEWS views and MT_NOALLOC_MAX_TILES tiles of the
  * context's batch tile shape; a batch beyond either limit is rejected with
  * MT_ERR_INVALID_ARG before anything is launched.  Nothing is staged in
